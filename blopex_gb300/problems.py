@@ -225,3 +225,25 @@ def stencil27_weights(nx: int, ny: int, nz: int, seed: int) -> np.ndarray:
 def mass_diagonal(n: int, seed: int) -> np.ndarray:
     """Lumped mass B = diag(U[0.5, 1.5]) (numpy PCG64, ``seed``)."""
     return np.random.default_rng(seed).uniform(0.5, 1.5, size=n)
+
+
+def stencil27_to_csr(nx: int, ny: int, nz: int, w: np.ndarray, shift: float):
+    """Assemble the shifted 27-point graph Laplacian as CSR (small checks)."""
+    n = nx * ny * nz
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    c = i + nx * (j + ny * k)
+    rows, cols, vals = [], [], []
+    diag = np.full(n, float(shift))
+    for e, (di, dj, dk) in enumerate(STENCIL27_OFFSETS):
+        i2, j2, k2 = i + di, j + dj, k + dk
+        ok = (i2 >= 0) & (i2 < nx) & (j2 >= 0) & (j2 < ny) & (k2 >= 0) & (k2 < nz)
+        a, b = c[ok], (i2 + nx * (j2 + ny * k2))[ok]
+        wv = np.asarray(w).reshape(n, 13)[a, e]
+        rows += [a, b]
+        cols += [b, a]
+        vals += [-wv, -wv]
+        np.add.at(diag, a, wv)
+        np.add.at(diag, b, wv)
+    rows.append(np.arange(n)); cols.append(np.arange(n)); vals.append(diag)
+    return coo_to_csr(n, np.concatenate(rows), np.concatenate(cols), np.concatenate(vals))

@@ -405,12 +405,25 @@ typedef struct {
   dpotrf_fn potrf;
 } lapack_t;
 
+/* Host-side fault injection for the failure-path tests: the Nth call
+   (1-based) of the Cholesky or of the generalized eigensolver reports
+   INFO = 1.  0 disables.  Mirrors ref_set_faults in ref_harness.c. */
+static int g_potrf_fail_at = 0, g_potrf_calls = 0;
+static int g_sygv_fail_at = 0, g_sygv_calls = 0;
+
+void oracle_set_faults(int potrf_fail_at, int sygv_fail_at)
+{
+  g_potrf_fail_at = potrf_fail_at;
+  g_sygv_fail_at = sygv_fail_at;
+}
+
 /* lobpcg.c:20-39 (Cholesky, upper) */
 static int chol_upper(const lapack_t* lp, double* a, int ld, int m)
 {
   char uplo = 'U';
   int info = 0;
   lp->potrf(&uplo, &m, a, &ld, &info);
+  if (++g_potrf_calls == g_potrf_fail_at && info == 0) info = 1;
   return info;
 }
 
@@ -419,7 +432,9 @@ static int gevp(const lapack_t* lp, double* a, double* b, int ld, int m, double*
 {
   int itype = 1, lwork = 10 * m, info = 0;
   char jobz = 'V', uplo = 'L';
-  double* work = (double*)calloc(lwork > 0 ? lwork : 1, sizeof(double));
+  double* work;
+  if (++g_sygv_calls == g_sygv_fail_at) return 1;
+  work = (double*)calloc(lwork > 0 ? lwork : 1, sizeof(double));
   lp->sygv(&itype, &jobz, &uplo, &m, a, &ld, b, &ld, w, work, &lwork, &info);
   free(work);
   return info;
@@ -488,6 +503,8 @@ int oracle_solve(long n, int k, oracle_op A, oracle_op B, oracle_op T,
 
   lp.sygv = (dsygv_fn)dsygv_ptr;
   lp.potrf = (dpotrf_fn)dpotrf_ptr;
+  g_potrf_calls = 0;
+  g_sygv_calls = 0;
   *iterations = 0;
 
   /* lobpcg.c:689-698 */

@@ -163,6 +163,7 @@ def lib():
             ctypes.c_void_p, ctypes.c_void_p,
             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
             ctypes.POINTER(ctypes.c_int)]
+        L.oracle_set_faults.argtypes = [ctypes.c_int, ctypes.c_int]
         L.oracle_apply.restype = None
         L.oracle_apply.argtypes = [ctypes.c_long, ctypes.c_int, _OpC,
                                    ctypes.c_void_p, ctypes.c_void_p]
@@ -187,8 +188,11 @@ class Result:
 
 def solve(A: Operator, x0: np.ndarray, B: Operator = NONE, T: Operator = NONE,
           Y: Optional[np.ndarray] = None, atol: float = 1e-6, rtol: float = 1e-50,
-          maxit: int = 100, history: bool = True) -> Result:
-    """Run the C restatement of lobpcg_solve_double (lobpcg.c:332-413)."""
+          maxit: int = 100, history: bool = True, potrf_fail_at: int = 0,
+          sygv_fail_at: int = 0) -> Result:
+    """Run the C restatement of lobpcg_solve_double (lobpcg.c:332-413).
+    ``potrf_fail_at``/``sygv_fail_at`` inject INFO = 1 into the Nth call of
+    the Cholesky / generalized eigensolver (host-side fault injection)."""
     x = np.array(x0, dtype=np.float64, order="F", copy=True)
     n, k = x.shape
     lam = np.zeros(max(k, 1))
@@ -199,11 +203,16 @@ def solve(A: Operator, x0: np.ndarray, B: Operator = NONE, T: Operator = NONE,
         Y = np.asfortranarray(Y, dtype=np.float64)
     it = ctypes.c_int(0)
     sygv, potrf = lapack_ptrs()
-    flag = lib().oracle_solve(n, k, _opc(A), _opc(B), _opc(T),
+    L = lib()
+    L.oracle_set_faults(potrf_fail_at, sygv_fail_at)
+    try:
+        flag = L.oracle_solve(n, k, _opc(A), _opc(B), _opc(T),
                               0 if Y is None else Y.shape[1], None if Y is None else _p(Y),
                               _p(x), atol, rtol, maxit, sygv, potrf,
                               _p(lam), _p(res), None if lh is None else _p(lh),
                               None if rh is None else _p(rh), ctypes.byref(it))
+    finally:
+        L.oracle_set_faults(0, 0)
     return Result(flag, it.value, x, lam[:k], res[:k], lh, rh)
 
 
@@ -239,9 +248,10 @@ def ref_lib():
             ctypes.c_void_p, ctypes.c_void_p,
             ctypes.c_int, ctypes.c_void_p,
             ctypes.c_int, ctypes.c_void_p,
-            ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+            ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
             ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.ref_set_faults.argtypes = [ctypes.c_int, ctypes.c_int]
         L.ref_set_lapack(*lapack_ptrs())
         _ref = L
     return _ref
@@ -255,7 +265,7 @@ def ref_random_block(n: int, k: int, seed: int) -> np.ndarray:
 
 def ref_solve(n: int, k: int, csr_arrays=None, dense_a=None, b_diag=None, t_diag=None,
               Y=None, seed: int = 0, x0=None, atol=1e-6, rtol=1e-50, maxit=100,
-              verbosity=0, potrf_fail_at=0) -> Result:
+              verbosity=0, potrf_fail_at=0, sygv_fail_at=0) -> Result:
     """Run the reference lobpcg_solve_double with the serial backend."""
     L = ref_lib()
     keep = []
@@ -279,9 +289,14 @@ def ref_solve(n: int, k: int, csr_arrays=None, dense_a=None, b_diag=None, t_diag
     rh = np.zeros((k, maxit + 1), order="F")
     it = ctypes.c_int(0)
     ny = 0 if Y is None else Y.shape[1]
-    flag = L.ref_solve(n, k, rp, ci, va, dn, arr(b_diag, np.float64), arr(t_diag, np.float64),
-                       ny, arr(Y, np.float64) if Y is not None else None,
-                       seed, arr(x0, np.float64) if x0 is not None else None,
-                       atol, rtol, maxit, verbosity, potrf_fail_at,
-                       _p(x), _p(lam), _p(res), _p(lh), _p(rh), ctypes.byref(it))
+    L.ref_set_faults(potrf_fail_at, sygv_fail_at)
+    try:
+        flag = L.ref_solve(n, k, rp, ci, va, dn, arr(b_diag, np.float64),
+                           arr(t_diag, np.float64),
+                           ny, arr(Y, np.float64) if Y is not None else None,
+                           seed, arr(x0, np.float64) if x0 is not None else None,
+                           atol, rtol, maxit, verbosity,
+                           _p(x), _p(lam), _p(res), _p(lh), _p(rh), ctypes.byref(it))
+    finally:
+        L.ref_set_faults(0, 0)
     return Result(flag, it.value, x, lam[:k], res[:k], lh, rh)

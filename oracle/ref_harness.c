@@ -58,16 +58,38 @@ static BlopexInt harness_dpotrf(char* uplo, BlopexInt* n, double* a,
   return 0;
 }
 
-/* Optional fault injection for the failure-path goldens: make the
-   Cholesky report failure on its Nth call (1-based); 0 disables. */
-static int g_potrf_fail_at = 0;
-static int g_potrf_calls = 0;
+/* Optional fault injection for the failure-path goldens: the Cholesky
+   (resp. the generalized eigensolver) reports INFO = 1 on its Nth call
+   (1-based); 0 disables. */
+static int g_potrf_fail_at = 0, g_potrf_calls = 0;
+static int g_sygv_fail_at = 0, g_sygv_calls = 0;
+
+void ref_set_faults(int potrf_fail_at, int sygv_fail_at)
+{
+  g_potrf_fail_at = potrf_fail_at;
+  g_sygv_fail_at = sygv_fail_at;
+}
+
 static BlopexInt harness_dpotrf_faulty(char* uplo, BlopexInt* n, double* a,
                                        BlopexInt* lda, BlopexInt* info)
 {
   g_potrf_calls++;
   g_dpotrf(uplo, n, a, lda, info);
   if (g_potrf_calls == g_potrf_fail_at && *info == 0) *info = 1;
+  return 0;
+}
+
+static BlopexInt harness_dsygv_faulty(BlopexInt* itype, char* jobz, char* uplo,
+                                      BlopexInt* n, double* a, BlopexInt* lda,
+                                      double* b, BlopexInt* ldb, double* w,
+                                      double* work, BlopexInt* lwork, BlopexInt* info)
+{
+  g_sygv_calls++;
+  if (g_sygv_calls == g_sygv_fail_at) {
+    *info = 1;
+    return 0;
+  }
+  g_dsygv(itype, jobz, uplo, n, a, lda, b, ldb, w, work, lwork, info);
   return 0;
 }
 
@@ -141,7 +163,6 @@ int ref_solve(int n, int k,
               int ny, const double* y,
               int seed, const double* x0,
               double atol, double rtol, int maxit, int verbosity,
-              int potrf_fail_at,
               double* x_out, double* lambda, double* resnorms,
               double* lambda_hist, double* res_hist, int* iterations)
 {
@@ -188,10 +209,10 @@ int ref_solve(int n, int k,
   td.n = n; td.d = t_diag;
 
   memset(&blap, 0, sizeof(blap));
-  blap.dsygv = harness_dsygv;
-  g_potrf_fail_at = potrf_fail_at;
   g_potrf_calls = 0;
-  blap.dpotrf = potrf_fail_at > 0 ? harness_dpotrf_faulty : harness_dpotrf;
+  g_sygv_calls = 0;
+  blap.dsygv = g_sygv_fail_at > 0 ? harness_dsygv_faulty : harness_dsygv;
+  blap.dpotrf = g_potrf_fail_at > 0 ? harness_dpotrf_faulty : harness_dpotrf;
   tol.absolute = atol;
   tol.relative = rtol;
 

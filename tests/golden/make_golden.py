@@ -1,0 +1,91 @@
+"""Generate the golden fixtures in this directory from the UNMODIFIED
+reference (test infrastructure).
+
+Runs the reference ``lobpcg_solve_double`` with the serial-double backend
+(compiled by ``oracle/Makefile`` into ``oracle/_ref``) on seeded synthetic
+inputs and records exit flag, iteration count, eigenvalues, residual norms
+and their histories.  Inputs are rebuilt by the tests from the same
+generators; a SHA-256 of every input array is stored to pin them.
+
+Run in a container that has the reference checkout:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from tests.golden import cases as C  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def capture_stdout(fn):
+    """Run fn() with the C-level stdout redirected; return (result, text)."""
+    sys.stdout.flush()
+    fd = os.dup(1)
+    with tempfile.TemporaryFile(mode="w+b") as tmp:
+        os.dup2(tmp.fileno(), 1)
+        try:
+            res = fn()
+        finally:
+            os.dup2(fd, 1)
+            os.close(fd)
+        tmp.seek(0)
+        text = tmp.read().decode()
+    return res, text
+
+
+def run_case(name: str) -> dict:
+    case = C.build(name)
+    kw = dict(seed=case.seed, x0=case.x0, atol=case.atol, rtol=case.rtol, maxit=case.maxit,
+              verbosity=case.verbosity, b_diag=case.b_diag, t_diag=case.t_diag, Y=case.Y,
+              potrf_fail_at=case.potrf_fail_at, sygv_fail_at=case.sygv_fail_at)
+    if case.csr is not None:
+        kw["csr_arrays"] = case.csr
+    else:
+        kw["dense_a"] = case.dense
+    r, text = capture_stdout(lambda: O.ref_solve(case.n, case.k, **kw))
+    ncol = r.iterations + 1
+    out = {
+        "name": name,
+        "description": case.description,
+        "n": case.n, "k": case.k,
+        "atol": case.atol, "rtol": case.rtol, "maxit": case.maxit,
+        "flag": r.flag, "iterations": r.iterations,
+        "lambda": r.lam.tolist(), "resnorm": r.res.tolist(),
+        "lambda_hist": r.lam_hist[:, :ncol].T.tolist() if case.k > 0 else [],
+        "res_hist": r.res_hist[:, :ncol].T.tolist() if case.k > 0 else [],
+        "inputs_sha256": {key: sha(val) for key, val in case.arrays().items()},
+    }
+    if case.verbosity:
+        out["stdout"] = text
+    if case.n * case.k <= 4000:
+        out["x"] = r.x.T.tolist()
+    return out
+
+
+def main():
+    if not O.have_ref():
+        O.build(ref=True)
+    for name in C.NAMES:
+        g = run_case(name)
+        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+            json.dump(g, f, indent=0)
+        print(f"{name}: flag {g['flag']} iterations {g['iterations']}")
+
+
+if __name__ == "__main__":
+    main()
