@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark of the LOBPCG hot path on GB300 (one JSON line on stdout).
+
+Workload (default, --config c2): the "plain FP64 on GPU" case -- 3D 7-point
+Dirichlet Laplacian 128^3 (n = 2,097,152, CSR int32 / FP64, nnz =
+14,581,760), block size k = 32, Jacobi preconditioner, X0 = 2*drand48()-1
+from seed 1, tolerance 1e-8, at most 300 iterations.  One step = one full
+lobpcg_solve_double call from X0 to exit (converged or maxit).  Synthetic
+data generated by the seeded builders in blopex_gb300/problems.py.
+
+value  = seconds per solve with X0, the matrix and the preconditioner
+         resident in HBM (max over ranks), CUDA events on the solver stream;
+e2e    = the same through the C ABI with X0 uploaded from pinned host memory
+         and the Ritz vectors + eigenvalues read back, every step;
+roofline = the kernel class with the largest share of the timed region,
+         from the library's CUDA-event timers (algorithmic bytes per launch /
+         event-timed duration), against MEASURED_PEAKS.json;
+cpu_baseline = the C restatement of the reference (oracle/, scalar loops,
+         one core) on a bounded sample, scaled to the full workload.
+
+--impl reference times that CPU implementation alone (the reference's own
+algorithm on the host cores; the compiled reference itself is not available
+on the GPU host).  Under torchrun each rank runs an independent replica
+(the solver does not shard: replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "c1": dict(kind="csr", grid=(20, 20, 20), k=10, seed=0, tol=1e-6, maxit=100, jacobi=False,
+               label="3D 7-point Laplacian 20^3 CSR, k=10, no preconditioner, tol 1e-6, maxit 100"),
+    "c2": dict(kind="csr", grid=(128, 128, 128), k=32, seed=1, tol=1e-8, maxit=300, jacobi=True,
+               label="3D 7-point Laplacian 128^3 CSR (n=2097152), k=32, Jacobi, tol 1e-8, maxit 300"),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_problem(cfg):
+    from blopex_gb300 import problems as P
+    nx, ny, nz = cfg["grid"]
+    n = nx * ny * nz
+    csr = P.laplacian3d_csr(nx, ny, nz)
+    x0 = P.drand48_block(n, cfg["k"], cfg["seed"])
+    tdiag = 1.0 / P.csr_diagonal(*csr) if cfg["jacobi"] else None
+    return n, csr, x0, tdiag
+
+
+def cpu_baseline(cfg, budget_s: float = 25.0):
+    """The oracle (C restatement of the reference, one core) on a bounded
+    sample: a 48^3 grid with the same k / preconditioner, 1 and 3 iterations;
+    the per-iteration time is scaled by n to the full grid."""
+    from blopex_gb300 import problems as P
+    from oracle import oracle as O
+    O.build(ref=False)
+    nx, ny, nz = cfg["grid"]
+    n_full = nx * ny * nz
+    s = min(48, nx)
+    n = s * s * s
+    csr = P.laplacian3d_csr(s, s, s)
+    x0 = P.drand48_block(n, cfg["k"], cfg["seed"])
+    A = O.csr(*csr)
+    T = O.diag(1.0 / P.csr_diagonal(*csr)) if cfg["jacobi"] else O.NONE
+    t0 = time.perf_counter()
+    O.solve(A, x0, T=T, atol=cfg["tol"], maxit=1, history=False)
+    t1 = time.perf_counter()
+    O.solve(A, x0, T=T, atol=cfg["tol"], maxit=3, history=False)
+    t2 = time.perf_counter()
+    per_it = max((t2 - t1) - (t1 - t0), 1e-9) / 2.0
+    setup = max((t1 - t0) - per_it, 0.0)
+    scale = n_full / n
+    value = (setup + cfg["maxit"] * per_it) * scale
+    return {"value": value, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"oracle C restatement, {s}^3 grid k={cfg['k']}, 1 and 3 iterations "
+                      f"({t2 - t0:.1f} s), per-iteration {per_it:.3f} s scaled by n x{scale:.1f} "
+                      f"to {cfg['maxit']} iterations (extrapolated)",
+            "per_iteration_s_full_n": per_it * scale}
+
+
+def run_reference(args, cfg):
+    """--impl reference: the CPU implementation of the path timed alone."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_baseline(cfg)
+    vals = [cpu_baseline(cfg) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": metric_name(cfg), "value": v, "unit": "s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(cfg, args), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def metric_name(cfg):
+    return ("time to k eigenpairs at resid 1e-8 (FP64 GPU path; mixed reported beside); "
+            "SpMM GB/s") if cfg["tol"] <= 1e-8 else "time to k eigenpairs"
+
+
+def config_block(cfg, args):
+    return {"workload": cfg["label"], "mode": args.mode, "n": int(np.prod(cfg["grid"])),
+            "k": cfg["k"], "maxit": args.maxit or cfg["maxit"], "tol": cfg["tol"],
+            "l2": "inputs larger than L2 (X alone is n*k*8 bytes)" if np.prod(cfg["grid"]) *
+                  cfg["k"] * 8 > 129e6 else "inputs smaller than L2", "parallelism":
+            "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--maxit", type=int, default=0, help="override maxit (exploration only)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision arm")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    cfg = dict(CONFIGS[args.config])
+    if args.maxit:
+        cfg["maxit"] = args.maxit
+
+    if args.impl == "reference":
+        run_reference(args, cfg)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from blopex_gb300 import solver as S
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    n, csr, x0, tdiag = build_problem(cfg)
+    k = cfg["k"]
+    ctx = S.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    A = S.CSRMatrix(ctx, *csr)
+    T = S.Diagonal(ctx, tdiag) if tdiag is not None else None
+    X = S.MultiVector(ctx, n, k)
+    X0 = S.MultiVector.from_host(ctx, x0)
+
+    def solve(mode):
+        ctx.set_options(precision=S.FP64 if mode == "fp64" else S.MIXED)
+        X.copy_from(X0)
+        return S.lobpcg_solve_double(X, A, T=T, atol=cfg["tol"], rtol=1e-50,
+                                     maxit=cfg["maxit"], history=False)
+
+    for _ in range(args.warmup):
+        solve(args.mode)
+
+    ctx.profiling(True)
+    ctx.reset_kernel_times()
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = ctx.lib.gpu_KernelLaunchCount()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    results = [solve(args.mode) for _ in range(args.steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.lib.gpu_KernelLaunchCount() - launches0
+    clocks = sampler.stop()
+    barrier()
+    ktimes = ctx.kernel_times()
+    ctx.profiling(False)
+    secs = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    if dist is not None:
+        t = torch.tensor([secs], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    res = results[-1]
+
+    # e2e: X0 from pinned host memory, Ritz vectors back, every step
+    pinned_in = torch.from_numpy(np.asfortranarray(x0).ravel(order="F")).pin_memory()
+    pinned_out = torch.empty(n * k, dtype=torch.float64).pin_memory()
+    ctx.set_options(precision=S.FP64 if args.mode == "fp64" else S.MIXED)
+    e2e_times = []
+    for _ in range(max(1, args.steps)):
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X.upload_ptr(pinned_in.data_ptr(), n)
+        r2 = S.lobpcg_solve_double(X, A, T=T, atol=cfg["tol"], rtol=1e-50, maxit=cfg["maxit"],
+                                   history=False)
+        X.download_ptr(pinned_out.data_ptr(), n)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = statistics.median(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = float(t.item())
+
+    # the mixed-precision arm on the same problem (one solve, timed)
+    mixed = None
+    if args.mode == "fp64" and not args.no_mixed:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rm = solve("mixed")
+        torch.cuda.synchronize()
+        tm = time.perf_counter() - t0
+        mixed = {"seconds": tm, "flag": rm.flag, "iterations": rm.iterations,
+                 "iterations_fp32": rm.stats["iterations_fp32"],
+                 "iterations_fp64": rm.stats["iterations_fp64"],
+                 "max_rel_lambda_diff_vs_fp64": float(np.max(np.abs(rm.lam - res.lam) /
+                                                             np.abs(res.lam))),
+                 "final_max_residual": float(np.max(rm.res))}
+
+    pk, pk_kind = peaks()
+    total_ms = sum(v["ms"] for v in ktimes.values()) or 1.0
+    dom_name, dom = max(ktimes.items(), key=lambda kv: kv[1]["ms"])
+    achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
+    roofline = {"kernel": dom_name, "bound": "hbm", "achieved": achieved,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "peak_kind": pk_kind, "traffic": None,
+                "share_of_kernel_time": dom["ms"] / total_ms,
+                "launches": dom["launches"], "avg_launch_ms": dom["ms"] / dom["launches"],
+                "achieved_tflops": dom["flops"] / (dom["ms"] / 1e3) / 1e12}
+    spmm = ktimes.get("spmm_csr")
+    kernels = {nm: {"share": v["ms"] / total_ms, "launches": v["launches"],
+                    "avg_ms": v["ms"] / v["launches"],
+                    "gbs": v["bytes"] / (v["ms"] / 1e3) / 1e9,
+                    "tflops": v["flops"] / (v["ms"] / 1e3) / 1e12}
+               for nm, v in sorted(ktimes.items(), key=lambda kv: -kv[1]["ms"])}
+
+    line = {"metric": metric_name(cfg), "value": secs, "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.mode == "fp64" else "f32+f64", "data": "synthetic",
+            "config": config_block(cfg, args),
+            "result": {"flag": res.flag, "iterations": res.iterations,
+                       "lambda_min": float(res.lam[0]), "lambda_max": float(res.lam[-1]),
+                       "max_residual": float(np.max(res.res))},
+            "roofline": roofline,
+            "spmm": None if spmm is None else {
+                "gbs": spmm["bytes"] / (spmm["ms"] / 1e3) / 1e9,
+                "frac_hbm": spmm["bytes"] / (spmm["ms"] / 1e3) / 1e9 / pk["hbm_gbs"],
+                "avg_launch_ms": spmm["ms"] / spmm["launches"]},
+            "kernels": kernels,
+            "mixed": mixed,
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": n * k * 8,
+                    "d2h_bytes_per_step": n * k * 8 + 2 * k * 8},
+            "gpu_launches": int(launches),
+            "clocks": clocks}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(cfg)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

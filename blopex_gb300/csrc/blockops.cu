@@ -1,0 +1,507 @@
+// blockops.cu -- tall-skinny block kernels on column-major multivectors
+// (CUDA-core versions, FP64 and FP32 storage):
+//   Gram        G = X' Y          (serial_Multi_VectorInnerProd, multi_vector.c:354-406)
+//   X*C update  Y = X C [+ Z]     (serial_Multi_VectorByMatrix, multi_vector.c:474-524)
+//   axpby, column scaling, column dots, residual, precision conversion,
+//   drand48 fill (multi_vector.c:165-184).
+// Columns are addressed through blk_cols pointer tables, so masked
+// (non-contiguous) columns and concatenated blocks [X R P] cost nothing.
+// Split-k partial sums are reduced in a fixed order: results are
+// deterministic run to run.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+#define CUDA_LAUNCH_CHECK(ctx, what) gb_cuda_check((ctx), (int)cudaGetLastError(), (what))
+
+static inline cudaStream_t S(gpu_Context* ctx) { return (cudaStream_t)ctx->stream; }
+
+// ------------------------------------------------------------------------
+// Gram: partial[s][j*h + i] = sum over rows of split s of X(r,i) * Y(r,j)
+// 256 threads as 16 x 16; each thread owns a TM x TN register tile with
+// rows ty + 16*a and columns tx + 16*b; rows are staged 32 at a time.
+// FP32 inputs accumulate in FP32 over 128-row blocks, flushed to FP64.
+// ------------------------------------------------------------------------
+template <typename T, int TM, int TN>
+__global__ void __launch_bounds__(256) gram_partial_kernel(blk_cols X, int h, blk_cols Y, int w,
+                                                           long n, long rows_per_split,
+                                                           double* __restrict__ partial)
+{
+  constexpr int BM = 16 * TM, BN = 16 * TN, RK = 32;
+  __shared__ T xs[RK][BM + 1];
+  __shared__ T ys[RK][BN + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int i0 = blockIdx.x * BM, j0 = blockIdx.y * BN;
+  const long r_begin = (long)blockIdx.z * rows_per_split;
+  const long r_end = min(n, r_begin + rows_per_split);
+
+  double acc[TM][TN];
+  T accs[TM][TN];
+#pragma unroll
+  for (int a = 0; a < TM; a++)
+#pragma unroll
+    for (int b = 0; b < TN; b++) {
+      acc[a][b] = 0.0;
+      accs[a][b] = T(0);
+    }
+
+  int chunk = 0;
+  for (long r0 = r_begin; r0 < r_end; r0 += RK) {
+    // stage rows r0..r0+RK of the BM columns of X and BN columns of Y
+    for (int e = threadIdx.x; e < RK * BM; e += 256) {
+      int rr = e % RK, cc = e / RK;
+      long r = r0 + rr;
+      int c = i0 + cc;
+      T v = T(0);
+      if (r < r_end && c < h) v = ((const T*)X.col[c])[r];
+      xs[rr][cc] = v;
+    }
+    for (int e = threadIdx.x; e < RK * BN; e += 256) {
+      int rr = e % RK, cc = e / RK;
+      long r = r0 + rr;
+      int c = j0 + cc;
+      T v = T(0);
+      if (r < r_end && c < w) v = ((const T*)Y.col[c])[r];
+      ys[rr][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int rr = 0; rr < RK; rr++) {
+      T xv[TM], yv[TN];
+#pragma unroll
+      for (int a = 0; a < TM; a++) xv[a] = xs[rr][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < TN; b++) yv[b] = ys[rr][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < TM; a++)
+#pragma unroll
+        for (int b = 0; b < TN; b++) accs[a][b] = fma(xv[a], yv[b], accs[a][b]);
+    }
+    __syncthreads();
+    if (sizeof(T) == 8 || (++chunk & 3) == 0) {
+#pragma unroll
+      for (int a = 0; a < TM; a++)
+#pragma unroll
+        for (int b = 0; b < TN; b++) {
+          acc[a][b] += (double)accs[a][b];
+          accs[a][b] = T(0);
+        }
+    }
+  }
+  double* out = partial + (size_t)blockIdx.z * h * w;
+#pragma unroll
+  for (int a = 0; a < TM; a++)
+#pragma unroll
+    for (int b = 0; b < TN; b++) {
+      int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < h && j < w) out[(size_t)j * h + i] = acc[a][b] + (double)accs[a][b];
+    }
+}
+
+__global__ void gram_reduce_kernel(const double* __restrict__ partial, int splits, int h, int w,
+                                   double* __restrict__ G, int ldg)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= h * w) return;
+  double s = 0.0;
+  for (int p = 0; p < splits; p++) s += partial[(size_t)p * h * w + e];
+  int i = e % h, j = e / h;
+  G[(size_t)j * ldg + i] = s;
+}
+
+template <typename T, int TM, int TN>
+static int gram_launch(gpu_Context* ctx, long n, const blk_cols* X, int h, const blk_cols* Y,
+                       int w, double* G, int ldg)
+{
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  int gx = (h + BM - 1) / BM, gy = (w + BN - 1) / BN;
+  int target = 2 * ctx->num_sms;
+  long splits = target / (gx * gy);
+  if (splits < 1) splits = 1;
+  long max_splits = (n + 255) / 256;
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  long rows = (n + splits - 1) / splits;
+  rows = (rows + 31) / 32 * 32;
+  splits = (n + rows - 1) / rows;
+  if (splits < 1) splits = 1;
+  double* partial = (double*)gb_workspace(ctx, sizeof(double) * (size_t)splits * h * w);
+  if (!partial) return -1;
+  dim3 grid(gx, gy, (unsigned)splits);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_GRAM);
+  gram_partial_kernel<T, TM, TN><<<grid, 256, 0, S(ctx)>>>(*X, h, *Y, w, n, rows, partial);
+  int tot = h * w;
+  gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, S(ctx)>>>(partial, (int)splits, h, w, G, ldg);
+  gb_prof_end(ctx, &pr, (double)sizeof(T) * n * (h + w), 2.0 * n * h * w);
+  gb_count_launch(2);
+  return CUDA_LAUNCH_CHECK(ctx, "gram");
+}
+
+extern "C" int gb_gram(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
+                       const blk_cols* Y, int w, double* G, int ldg)
+{
+  if (h <= 0 || w <= 0) return 0;
+  if (dtype == GPU_MV_FLOAT64) {
+    if (h <= 32 && w <= 32) return gram_launch<double, 2, 2>(ctx, n, X, h, Y, w, G, ldg);
+    return gram_launch<double, 4, 4>(ctx, n, X, h, Y, w, G, ldg);
+  }
+  if (h <= 32 && w <= 32) return gram_launch<float, 2, 2>(ctx, n, X, h, Y, w, G, ldg);
+  return gram_launch<float, 4, 4>(ctx, n, X, h, Y, w, G, ldg);
+}
+
+// ------------------------------------------------------------------------
+// X*C update: Y(:, j0:j0+32) for 64 rows per CTA; thread t owns row t%64
+// and 8 columns (t/64)*8 ... ; K staged 32 at a time in shared memory.
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) bymat_kernel(blk_cols X, int h, const double* __restrict__ C,
+                                                    int ldc, blk_cols Y, int w, blk_cols Z,
+                                                    int has_z, long n)
+{
+  constexpr int BM = 64, BN = 32, KC = 32;
+  __shared__ T xs[KC][BM];
+  __shared__ T cs[KC][BN];
+  const int t = threadIdx.x;
+  const int rl = t & 63, cg = t >> 6;
+  const long r0 = (long)blockIdx.x * BM;
+  const int j0 = blockIdx.y * BN;
+  T acc[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) acc[b] = T(0);
+
+  for (int k0 = 0; k0 < h; k0 += KC) {
+    for (int e = t; e < KC * BM; e += 256) {
+      int rr = e % BM, kk = e / BM;
+      long r = r0 + rr;
+      T v = T(0);
+      if (r < n && k0 + kk < h) v = ((const T*)X.col[k0 + kk])[r];
+      xs[kk][rr] = v;
+    }
+    for (int e = t; e < KC * BN; e += 256) {
+      int kk = e % KC, jj = e / KC;
+      T v = T(0);
+      if (k0 + kk < h && j0 + jj < w) v = (T)C[(size_t)(j0 + jj) * ldc + k0 + kk];
+      cs[kk][jj] = v;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < KC; kk++) {
+      T xv = xs[kk][rl];
+#pragma unroll
+      for (int b = 0; b < 8; b++) acc[b] = fma(xv, cs[kk][cg * 8 + b], acc[b]);
+    }
+    __syncthreads();
+  }
+  long r = r0 + rl;
+  if (r < n) {
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+      int j = j0 + cg * 8 + b;
+      if (j < w) {
+        T v = acc[b];
+        if (has_z) v += ((const T*)Z.col[j])[r];
+        ((T*)Y.col[j])[r] = v;
+      }
+    }
+  }
+}
+
+extern "C" int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
+                        const double* C, int ldc, const blk_cols* Y, int w, const blk_cols* Z)
+{
+  if (w <= 0 || n <= 0) return 0;
+  dim3 grid((unsigned)((n + 63) / 64), (w + 31) / 32);
+  blk_cols empty;
+  const blk_cols* z = Z ? Z : &empty;
+  const double es = dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0;
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_XC);
+  if (dtype == GPU_MV_FLOAT64)
+    bymat_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n);
+  else
+    bymat_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n);
+  gb_prof_end(ctx, &pr, es * n * (h + w + (Z ? w : 0)), 2.0 * n * h * w);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "bymat");
+}
+
+// ------------------------------------------------------------------------
+// elementwise column kernels: grid.y = column, grid-stride over rows
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void axpby_kernel(blk_cols X, double alpha, blk_cols Y, double beta, long n)
+{
+  const T* x = (const T*)X.col[blockIdx.y];
+  T* y = (T*)Y.col[blockIdx.y];
+  const T a = (T)alpha, b = (T)beta;
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    if (beta == 0.0)
+      y[r] = a * x[r];
+    else
+      y[r] = a * x[r] + b * y[r];
+  }
+}
+
+static unsigned row_blocks(gpu_Context* ctx, long n, int w)
+{
+  long want = (n + 255) / 256;
+  long cap = (long)ctx->num_sms * 8 / (w > 0 ? w : 1);
+  if (cap < 4) cap = 4;
+  if (want > cap) want = cap;
+  if (want < 1) want = 1;
+  return (unsigned)want;
+}
+
+extern "C" int gb_axpby(gpu_Context* ctx, int dtype, long n, double alpha, const blk_cols* X,
+                        double beta, const blk_cols* Y, int w)
+{
+  if (w <= 0 || n <= 0) return 0;
+  dim3 grid(row_blocks(ctx, n, w), w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_BLAS1);
+  if (dtype == GPU_MV_FLOAT64)
+    axpby_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, alpha, *Y, beta, n);
+  else
+    axpby_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, alpha, *Y, beta, n);
+  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * w * (beta == 0.0 ? 2 : 3), 0.0);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "axpby");
+}
+
+struct idx_table {
+  int v[BLK_MAXCOLS];
+};
+
+template <typename T>
+__global__ void scale_cols_kernel(blk_cols X, const double* __restrict__ d, idx_table idx,
+                                  blk_cols Y, long n)
+{
+  const T* x = (const T*)X.col[blockIdx.y];
+  T* y = (T*)Y.col[blockIdx.y];
+  const T a = (T)d[idx.v[blockIdx.y]];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    y[r] = a * x[r];
+}
+
+static void fill_idx(idx_table* t, const int* idx, int w)
+{
+  for (int j = 0; j < w; j++) t->v[j] = idx ? idx[j] : j;
+}
+
+extern "C" int gb_scale_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X,
+                             const double* d, const int* idx, const blk_cols* Y, int w)
+{
+  if (w <= 0 || n <= 0) return 0;
+  idx_table t;
+  fill_idx(&t, idx, w);
+  dim3 grid(row_blocks(ctx, n, w), w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_BLAS1);
+  if (dtype == GPU_MV_FLOAT64)
+    scale_cols_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, d, t, *Y, n);
+  else
+    scale_cols_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, d, t, *Y, n);
+  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * w * 2, 0.0);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "scale_cols");
+}
+
+// column dot products: per-CTA partial sums, then a fixed-order reduction
+template <typename T>
+__global__ void dot_partial_kernel(blk_cols X, blk_cols Y, long n, double* __restrict__ partial)
+{
+  const T* x = (const T*)X.col[blockIdx.y];
+  const T* y = (const T*)Y.col[blockIdx.y];
+  double s = 0.0;
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    s += (double)x[r] * (double)y[r];
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+__global__ void dot_reduce_kernel(const double* __restrict__ partial, int nb, idx_table idx,
+                                  int w, double* __restrict__ out)
+{
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= w) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; b++) s += partial[(size_t)j * nb + b];
+  out[idx.v[j]] = s;
+}
+
+extern "C" int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X,
+                           const blk_cols* Y, int w, double* out, const int* idx)
+{
+  if (w <= 0) return 0;
+  idx_table t;
+  fill_idx(&t, idx, w);
+  unsigned nb = row_blocks(ctx, n, w);
+  double* partial = (double*)gb_workspace(ctx, sizeof(double) * (size_t)nb * w);
+  if (!partial) return -1;
+  dim3 grid(nb, w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_BLAS1);
+  if (dtype == GPU_MV_FLOAT64)
+    dot_partial_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n, partial);
+  else
+    dot_partial_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n, partial);
+  dot_reduce_kernel<<<(w + 63) / 64, 64, 0, S(ctx)>>>(partial, nb, t, w, out);
+  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * w * 2, 2.0 * n * w);
+  gb_count_launch(2);
+  return CUDA_LAUNCH_CHECK(ctx, "dot_cols");
+}
+
+// fused residual R = lambda*BX - AX with squared column norms
+template <typename T>
+__global__ void residual_partial_kernel(blk_cols BX, blk_cols AX, const double* __restrict__ lambda,
+                                        idx_table idx, blk_cols R, long n,
+                                        double* __restrict__ partial)
+{
+  const T* bx = (const T*)BX.col[blockIdx.y];
+  const T* ax = (const T*)AX.col[blockIdx.y];
+  T* rr = (T*)R.col[blockIdx.y];
+  const T lam = (T)lambda[idx.v[blockIdx.y]];
+  double s = 0.0;
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    T v = lam * bx[r] - ax[r];
+    rr[r] = v;
+    s += (double)v * (double)v;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+extern "C" int gb_residual(gpu_Context* ctx, int dtype, long n, const blk_cols* BX,
+                           const blk_cols* AX, const double* lambda, const int* idx,
+                           const blk_cols* R, int w, double* norm2)
+{
+  if (w <= 0) return 0;
+  idx_table t;
+  fill_idx(&t, idx, w);
+  unsigned nb = row_blocks(ctx, n, w);
+  double* partial = (double*)gb_workspace(ctx, sizeof(double) * (size_t)nb * w);
+  if (!partial) return -1;
+  dim3 grid(nb, w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_RESID);
+  if (dtype == GPU_MV_FLOAT64)
+    residual_partial_kernel<double><<<grid, 256, 0, S(ctx)>>>(*BX, *AX, lambda, t, *R, n, partial);
+  else
+    residual_partial_kernel<float><<<grid, 256, 0, S(ctx)>>>(*BX, *AX, lambda, t, *R, n, partial);
+  dot_reduce_kernel<<<(w + 63) / 64, 64, 0, S(ctx)>>>(partial, nb, t, w, norm2);
+  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * w * 3, 4.0 * n * w);
+  gb_count_launch(2);
+  return CUDA_LAUNCH_CHECK(ctx, "residual");
+}
+
+template <typename TI, typename TO>
+__global__ void convert_kernel(blk_cols X, blk_cols Y, long n)
+{
+  const TI* x = (const TI*)X.col[blockIdx.y];
+  TO* y = (TO*)Y.col[blockIdx.y];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    y[r] = (TO)x[r];
+}
+
+extern "C" int gb_convert(gpu_Context* ctx, long n, int dtype_x, const blk_cols* X, int dtype_y,
+                          const blk_cols* Y, int w)
+{
+  if (w <= 0 || n <= 0) return 0;
+  dim3 grid(row_blocks(ctx, n, w), w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_BLAS1);
+  if (dtype_x == GPU_MV_FLOAT64 && dtype_y == GPU_MV_FLOAT32)
+    convert_kernel<double, float><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n);
+  else if (dtype_x == GPU_MV_FLOAT32 && dtype_y == GPU_MV_FLOAT64)
+    convert_kernel<float, double><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n);
+  else if (dtype_x == GPU_MV_FLOAT64)
+    convert_kernel<double, double><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n);
+  else
+    convert_kernel<float, float><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n);
+  gb_prof_end(ctx, &pr, ((dtype_x == GPU_MV_FLOAT64 ? 8.0 : 4.0) + (dtype_y == GPU_MV_FLOAT64 ? 8.0 : 4.0)) * n * w, 0.0);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "convert");
+}
+
+// ------------------------------------------------------------------------
+// drand48: state_{t+1} = a*state_t + c mod 2^48 with a = 0x5DEECE66D,
+// c = 0xB, state_0 = (seed << 16) | 0x330E, value = state / 2^48.
+// Element e of the fill (column-major over the listed columns) uses state
+// e+1; each thread jumps ahead with the affine-map powers (mod 2^64
+// arithmetic is exact mod 2^48).
+// ------------------------------------------------------------------------
+struct lcg_table {
+  unsigned long long a[48], c[48];  // map for 2^b steps
+};
+
+__device__ __forceinline__ unsigned long long lcg_jump(const lcg_table& t, unsigned long long s,
+                                                       unsigned long long steps)
+{
+  const unsigned long long M = (1ULL << 48) - 1;
+  for (int b = 0; b < 48 && steps; b++, steps >>= 1)
+    if (steps & 1) s = (t.a[b] * s + t.c[b]) & M;
+  return s;
+}
+
+template <typename T>
+__global__ void drand48_kernel(T* data, long n, long ld, idx_table idx, int w,
+                               unsigned long long state0, lcg_table tab)
+{
+  const unsigned long long M = (1ULL << 48) - 1;
+  const unsigned long long A = 0x5DEECE66DULL, Cc = 0xBULL;
+  long total = n * (long)w;
+  long per = 64;  // consecutive values per thread
+  long first = (blockIdx.x * (long)blockDim.x + threadIdx.x) * per;
+  if (first >= total) return;
+  unsigned long long s = lcg_jump(tab, state0, (unsigned long long)first);
+  long last = min(total, first + per);
+  for (long e = first; e < last; e++) {
+    s = (A * s + Cc) & M;
+    double v = (double)s * (1.0 / 281474976710656.0);
+    long c = e / n, r = e - c * n;
+    data[(long)idx.v[c] * ld + r] = (T)(2.0 * v - 1.0);
+  }
+}
+
+extern "C" int gb_drand48_fill(gpu_Context* ctx, int dtype, void* data, long n, long ld,
+                               const int* idx, int w, unsigned int seed)
+{
+  if (w <= 0 || n <= 0) return 0;
+  idx_table t;
+  fill_idx(&t, idx, w);
+  lcg_table tab;
+  const unsigned long long M = (1ULL << 48) - 1;
+  unsigned long long a = 0x5DEECE66DULL, c = 0xBULL;
+  for (int b = 0; b < 48; b++) {
+    tab.a[b] = a;
+    tab.c[b] = c;
+    // compose the map with itself: s -> a(a s + c) + c
+    unsigned long long a2 = (a * a) & M, c2 = (a * c + c) & M;
+    a = a2;
+    c = c2;
+  }
+  unsigned long long state0 = (((unsigned long long)seed) << 16) | 0x330EULL;
+  long total = n * (long)w;
+  long threads = (total + 63) / 64;
+  unsigned blocks = (unsigned)((threads + 255) / 256);
+  if (dtype == GPU_MV_FLOAT64)
+    drand48_kernel<double><<<blocks, 256, 0, S(ctx)>>>((double*)data, n, ld, t, w, state0, tab);
+  else
+    drand48_kernel<float><<<blocks, 256, 0, S(ctx)>>>((float*)data, n, ld, t, w, state0, tab);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "drand48_fill");
+}

@@ -1,0 +1,141 @@
+/*
+ * internal.h -- shared declarations of the GB300 LOBPCG library (not part
+ * of the public C ABI).  Included by the C host driver and the CUDA files.
+ */
+#ifndef BLOPEX_GB300_INTERNAL_H
+#define BLOPEX_GB300_INTERNAL_H
+
+#include <stddef.h>
+#include "lobpcg_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* widest block handed to one kernel: [X R P] for k = 128 */
+#define BLK_MAXCOLS 384
+
+/* Column pointer table passed by value to the block kernels: logical
+   column c of an operand lives at col[c] (device address, `len` rows). */
+typedef struct {
+  const void* col[BLK_MAXCOLS];
+} blk_cols;
+
+/* kernel classes for the event timers */
+enum {
+  GB_K_GRAM = 0, GB_K_XC, GB_K_CSR, GB_K_ST7, GB_K_ST5, GB_K_ST27, GB_K_DIAG, GB_K_RESID,
+  GB_K_BLAS1, GB_K_CHOLQR, GB_K_SYGV, GB_K_SMALL, GB_K_TC_GRAM, GB_K_TC_XC, GB_K_COUNT
+};
+
+typedef struct {
+  void* start; /* cudaEvent_t */
+  void* stop;
+  int cls;
+  double bytes, flops;
+} gb_prof_rec;
+
+struct gpu_Context {
+  int device;
+  void* stream;       /* cudaStream_t */
+  int owns_stream;
+  lobpcg_gpu_options opt;
+  lobpcg_gpu_stats stats;
+  char err[512];
+  /* grow-only device scratch for split-k partials and small matrices */
+  void* work;
+  size_t work_bytes;
+  /* pinned host staging for small device->host reads */
+  void* pinned;
+  size_t pinned_bytes;
+  int num_sms;
+  /* host-side fault injection counters (see lobpcg_gpu_options) */
+  int potrf_calls;
+  int sygv_calls;
+  /* kernel timers */
+  int profile;
+  gb_prof_rec* prof_pending;
+  int prof_npending, prof_cap;
+  void** prof_pool; /* free cudaEvent_t */
+  int prof_npool;
+  lobpcg_gpu_kernel_time prof[GB_K_COUNT];
+};
+
+/* error helpers (context.cu) */
+int gb_fail(gpu_Context* ctx, const char* fmt, ...);
+int gb_cuda_check(gpu_Context* ctx, int cuda_status, const char* what);
+void* gb_workspace(gpu_Context* ctx, size_t bytes);
+void* gb_pinned(gpu_Context* ctx, size_t bytes);
+void gb_count_launch(long long n);
+int gb_memcpy_d2h(gpu_Context* ctx, void* dst, const void* src, size_t bytes);
+int gb_memcpy_h2d(gpu_Context* ctx, void* dst, const void* src, size_t bytes);
+int gb_memcpy_d2d(gpu_Context* ctx, void* dst, const void* src, size_t bytes);
+int gb_sync(gpu_Context* ctx);
+void* gb_device_alloc(gpu_Context* ctx, size_t bytes);
+void gb_device_free(void* p);
+double gb_now(void);
+/* bracket one kernel launch (no-ops unless profiling is on) */
+void gb_prof_begin(gpu_Context* ctx, gb_prof_rec* rec, int cls);
+void gb_prof_end(gpu_Context* ctx, gb_prof_rec* rec, double bytes, double flops);
+/* fold finished timers into ctx->prof (synchronises the stream) */
+void gb_prof_collect(gpu_Context* ctx);
+
+/* multivector helpers (multivector.cu) */
+int gb_is_gpu_interpreter(const mv_InterfaceInterpreter* ii);
+void gb_mv_set_mask_host(gpu_MultiVector* x, const BlopexInt* mask);
+int gb_mv_sync_mask(gpu_MultiVector* x);
+gpu_MultiVector* gb_mv_create_like(const gpu_MultiVector* x, int dtype);
+int gb_mv_fill_cols(const gpu_MultiVector* x, blk_cols* t, int offset);
+
+/* ---------------- block kernels (blockops.cu) ---------------- */
+/* G(0:h,0:w) (column-major, leading dimension ldg, FP64, device) =
+   X(:,0:h)' * Y(:,0:w); X and Y share dtype. */
+int gb_gram(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h, const blk_cols* Y,
+            int w, double* G, int ldg);
+/* Y(:,j) = sum_i X(:,i) C(i,j) [+ Z(:,j)], C FP64 device column-major (ldc) */
+int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h, const double* C,
+             int ldc, const blk_cols* Y, int w, const blk_cols* Z);
+/* Y(:,j) = alpha * X(:,j) + beta * Y(:,j) for j < w */
+int gb_axpby(gpu_Context* ctx, int dtype, long n, double alpha, const blk_cols* X, double beta,
+             const blk_cols* Y, int w);
+/* Y(:,j) = d[idx[j]] * X(:,j) (d FP64 device; idx host) */
+int gb_scale_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X, const double* d,
+                  const int* idx, const blk_cols* Y, int w);
+/* out[idx[j]] = X(:,j)' Y(:,j) (FP64 device) */
+int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X, const blk_cols* Y, int w,
+                double* out, const int* idx);
+/* Y(:,j) (dtype_y) = X(:,j) (dtype_x), converting precision */
+int gb_convert(gpu_Context* ctx, long n, int dtype_x, const blk_cols* X, int dtype_y,
+               const blk_cols* Y, int w);
+/* fused residual: R(:,j) = lambda[idx[j]] * BX(:,j) - AX(:,j); norm2[idx[j]] = |R(:,j)|^2 */
+int gb_residual(gpu_Context* ctx, int dtype, long n, const blk_cols* BX, const blk_cols* AX,
+                const double* lambda, const int* idx, const blk_cols* R, int w, double* norm2);
+/* drand48-compatible fill of column-major storage, columns listed in idx */
+int gb_drand48_fill(gpu_Context* ctx, int dtype, void* data, long n, long ld, const int* idx,
+                    int w, unsigned int seed);
+
+/* ---------------- small dense FP64 (dense.cu) ---------------- */
+/* in place: A(0:m,0:m) upper Cholesky factor U (A = U'U from the upper
+   triangle), then A <- inv(U) with the strict lower part cleared; *info
+   (device int) = 0 or the order of the first non-positive leading minor */
+int gb_cholqr_factor(gpu_Context* ctx, double* A, int ld, int m, int* info);
+/* generalized symmetric-definite eigenproblem A v = w B v (itype 1, lower
+   triangles read): A <- eigenvectors (B-orthonormal, ascending), w <- values,
+   B <- its lower Cholesky factor; *info as dsygv */
+int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w, int* info);
+/* small helpers on device matrices */
+int gb_small_symmetrize(gpu_Context* ctx, double* A, int ld, int m);
+int gb_small_identity(gpu_Context* ctx, double* A, int ld, int h, int w);
+int gb_small_diag(gpu_Context* ctx, double* A, int ld, int m, const double* d);
+/* C(0:h,0:w) = op(A) op(B), inner dimension l (constraints path) */
+int gb_small_gemm(gpu_Context* ctx, const double* A, int lda, int ta, const double* B, int ldb,
+                  int tb, double* C, int ldc, int h, int w, int l);
+
+/* ---------------- operators (operators.cu) ---------------- */
+struct gpu_Operator;
+int gb_operator_apply(struct gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,852 @@
+/*
+ * lobpcg_driver.c -- the host side of the GB300 LOBPCG solver (C).
+ *
+ * lobpcg_solve_double() keeps the reference's signature and semantics
+ * (blopex_abstract/krylov/lobpcg.c:332-413 and 502-1388) and runs the
+ * iteration on the device:
+ *   - the block vectors are gpu_MultiVector objects (column-major, device);
+ *   - Gram products, X*C updates, residuals and norms are device kernels;
+ *   - the 3k x 3k Gram matrices gramA/gramB, the Cholesky-QR factors and the
+ *     Rayleigh-Ritz eigenproblem stay in device memory (FP64);
+ *   - per iteration only the eigenvalues, residual norms and factorisation
+ *     status words come back to the host (for the soft-locking test, the
+ *     histories and the caller's arrays).
+ *
+ * One iteration performs the same operations, on the same gramA/gramB
+ * layout, as the reference loop (lobpcg.c:965-1318): implicit identities
+ * XAX = diag(lambda), XBX = RBR = PBP = I, lower blocks computed, Cholesky-QR
+ * of R and P with the sizeP = 0 restart when P's factorisation fails, and
+ * the same coordinate blocks of the Ritz vectors.
+ *
+ * Precision (lobpcg_gpu_options.precision):
+ *   FP64  -- every block in FP64 (the reference's arithmetic);
+ *   MIXED -- the iteration first runs on FP32 copies of the blocks (Gram
+ *            sums accumulated in FP64, small matrices in FP64) until the
+ *            largest residual drops below opt.fp64_below or stops improving;
+ *            the block is then promoted to FP64, re-orthonormalised and
+ *            Rayleigh-Ritz'ed in FP64 (the FP64 residual check), and the
+ *            iteration continues in FP64 until the tolerance is met.
+ */
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "internal.h"
+
+mv_InterfaceInterpreter* gb_mv_interpreter(mv_MultiVectorPtr x);
+
+typedef void (*op_fn)(void*, void*, void*);
+
+typedef struct {
+  gpu_Context* ctx;
+  long n;
+  int k, ny, k3;
+  int dt; /* dtype of the current phase */
+  int noB, noT, noY;
+  void *Adata, *Bdata, *Tdata;
+  op_fn A, B, T;
+  gpu_MultiVector *X, *R, *P, *W, *AX, *AR, *AP, *BX, *BR, *BP, *Y, *BY;
+  /* device small matrices */
+  double *gA, *gB, *lamAB, *lam, *norm2, *gYBY, *gYBX, *tYBX;
+  int* info;
+  /* host */
+  double* h_lam;
+  double* h_norm;
+  int* mask;
+  int verbosity;
+  lobpcg_Tolerance tol;
+} solver_t;
+
+static void err_message(int verbosity, const char* msg)
+{
+  if (verbosity) {
+    fprintf(stderr, "Error in LOBPCG:\n");
+    fputs(msg, stderr);
+  }
+}
+
+static void dump_lambda(const double* norms, const double* lam, int it, int k)
+{
+  printf("\n");
+  printf("Eigenvalue lambda       Residual              \n");
+  for (int i = 0; i < k; i++) printf("%22.14e  %22.14e\n", lam[i], fabs(norms[i]));
+  printf("\n%d iterations\n", it);
+}
+
+static double max_value(const double* v, int k)
+{
+  double m = v[0];
+  for (int i = 1; i < k; i++)
+    if (v[i] > m) m = v[i];
+  return m;
+}
+
+/* ----------------------------------------------------------- block ops */
+
+static void cols(const gpu_MultiVector* x, blk_cols* t) { gb_mv_fill_cols(x, t, 0); }
+
+static int d_copy(solver_t* s, gpu_MultiVector* x, gpu_MultiVector* y)
+{
+  blk_cols a, b;
+  if (x->num_active != y->num_active) return gb_fail(s->ctx, "copy: width mismatch");
+  cols(x, &a);
+  cols(y, &b);
+  return gb_convert(s->ctx, s->n, x->dtype, &a, y->dtype, &b, x->num_active);
+}
+
+static int d_axpy(solver_t* s, double alpha, gpu_MultiVector* x, gpu_MultiVector* y)
+{
+  blk_cols a, b;
+  if (x->num_active != y->num_active) return gb_fail(s->ctx, "axpy: width mismatch");
+  cols(x, &a);
+  cols(y, &b);
+  return gb_axpby(s->ctx, x->dtype, s->n, alpha, &a, 1.0, &b, x->num_active);
+}
+
+/* G(0:h, 0:w) = x(active)' y(active), leading dimension ldg */
+static int d_gram(solver_t* s, gpu_MultiVector* x, gpu_MultiVector* y, double* G, int ldg)
+{
+  blk_cols a, b;
+  cols(x, &a);
+  cols(y, &b);
+  return gb_gram(s->ctx, x->dtype, s->n, &a, x->num_active, &b, y->num_active, G, ldg);
+}
+
+/* y(active, w = y->num_active) = x(active, h = x->num_active) * C */
+static int d_bymat(solver_t* s, gpu_MultiVector* x, const double* C, int ldc, gpu_MultiVector* y)
+{
+  blk_cols a, b;
+  cols(x, &a);
+  cols(y, &b);
+  return gb_bymat(s->ctx, x->dtype, s->n, &a, x->num_active, C, ldc, &b, y->num_active, NULL);
+}
+
+/* apply an operator callback to the active columns of x -> y */
+static int d_apply(solver_t* s, op_fn op, void* data, gpu_MultiVector* x, gpu_MultiVector* y)
+{
+  gpu_Context* ctx = s->ctx;
+  if (op == gpu_OperatorApply) {
+    ctx->err[0] = 0;
+    op(data, x, y);
+    return ctx->err[0] ? -1 : 0;
+  }
+  /* a caller-supplied callback may launch on any stream: order it with the
+     solver's stream on both sides */
+  if (gb_mv_sync_mask(x) || gb_mv_sync_mask(y) || gb_sync(ctx)) return -1;
+  op(data, x, y);
+  return gb_cuda_check(ctx, (int)cudaDeviceSynchronize(), "operator callback");
+}
+
+/* norms of the residual columns listed by mask (all when mask == NULL):
+   host h_norm[i] = sqrt(|r_i' r_i|) (lobpcg.c:237-260) */
+static int d_resnorms(solver_t* s, gpu_MultiVector* r, const int* mask)
+{
+  int idx[BLK_MAXCOLS], na = 0;
+  blk_cols a;
+  for (int i = 0; i < s->k; i++)
+    if (!mask || mask[i]) idx[na++] = i;
+  if (na != r->num_active) return gb_fail(s->ctx, "residual norms: mask mismatch");
+  cols(r, &a);
+  if (gb_dot_cols(s->ctx, r->dtype, s->n, &a, &a, na, s->norm2, idx)) return -1;
+  double* tmp = (double*)gb_pinned(s->ctx, sizeof(double) * s->k);
+  if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->norm2, sizeof(double) * s->k)) return -1;
+  for (int c = 0; c < na; c++) s->h_norm[idx[c]] = sqrt(fabs(tmp[idx[c]]));
+  return 0;
+}
+
+/* r(active) = bx(active) * diag(lambda(mask)) (lobpcg.c:1277-1279) */
+static int d_bydiag_lambda(solver_t* s, gpu_MultiVector* bx, const int* mask, gpu_MultiVector* r)
+{
+  int idx[BLK_MAXCOLS], na = 0;
+  blk_cols a, b;
+  for (int i = 0; i < s->k; i++)
+    if (!mask || mask[i]) idx[na++] = i;
+  if (na != bx->num_active || na != r->num_active)
+    return gb_fail(s->ctx, "bydiag: mask mismatch");
+  cols(bx, &a);
+  cols(r, &b);
+  return gb_scale_cols(s->ctx, bx->dtype, s->n, &a, s->lam, idx, &b, na);
+}
+
+static int read_info(solver_t* s, int* info)
+{
+  int* tmp = (int*)gb_pinned(s->ctx, sizeof(int));
+  if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->info, sizeof(int))) return -1;
+  *info = *tmp;
+  return 0;
+}
+
+/* B-orthonormalise x given bx = B x, r = the Gram block (lobpcg.c:197-232).
+   *info: 0 or the Cholesky failure order.  Returns -1 on a CUDA error. */
+static int d_implicit_qr(solver_t* s, gpu_MultiVector* x, gpu_MultiVector* bx, double* r, int ld,
+                         gpu_MultiVector* z, int* info)
+{
+  const int m = x->num_active;
+  if (d_gram(s, x, bx, r, ld)) return -1;
+  if (gb_cholqr_factor(s->ctx, r, ld, m, s->info)) return -1;
+  if (read_info(s, info)) return -1;
+  if (*info) return 0;
+  if (d_copy(s, x, z)) return -1;
+  return d_bymat(s, z, r, ld, x);
+}
+
+static int d_sygv(solver_t* s, int m, double* w, int* info)
+{
+  if (gb_sygv(s->ctx, s->gA, s->gB, s->k3, m, w, s->info)) return -1;
+  return read_info(s, info);
+}
+
+static int fetch_lambda(solver_t* s)
+{
+  double* tmp = (double*)gb_pinned(s->ctx, sizeof(double) * s->k);
+  if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->lam, sizeof(double) * s->k)) return -1;
+  memcpy(s->h_lam, tmp, sizeof(double) * s->k);
+  return 0;
+}
+
+/* -------------------------------------------------------- allocation */
+
+static void free_blocks(solver_t* s)
+{
+  gpu_MultiVector** b[] = {&s->R, &s->P, &s->W, &s->AX, &s->AR, &s->AP};
+  for (size_t i = 0; i < sizeof(b) / sizeof(b[0]); i++) {
+    gpu_MultiVectorDestroy(*b[i]);
+    *b[i] = NULL;
+  }
+  if (!s->noB) {
+    gpu_MultiVectorDestroy(s->BX);
+    gpu_MultiVectorDestroy(s->BR);
+    gpu_MultiVectorDestroy(s->BP);
+    if (!s->noY) gpu_MultiVectorDestroy(s->BY);
+  }
+  s->BX = s->BR = s->BP = s->BY = NULL;
+}
+
+static int alloc_blocks(solver_t* s, gpu_MultiVector* X)
+{
+  gpu_Context* ctx = s->ctx;
+  s->X = X;
+  s->dt = X->dtype;
+  s->R = gb_mv_create_like(X, s->dt);
+  s->P = gb_mv_create_like(X, s->dt);
+  s->W = gb_mv_create_like(X, s->dt);
+  s->AX = gb_mv_create_like(X, s->dt);
+  s->AR = gb_mv_create_like(X, s->dt);
+  s->AP = gb_mv_create_like(X, s->dt);
+  if (!s->R || !s->P || !s->W || !s->AX || !s->AR || !s->AP) return gb_fail(ctx, "out of device memory");
+  if (!s->noB) {
+    s->BX = gb_mv_create_like(X, s->dt);
+    s->BR = gb_mv_create_like(X, s->dt);
+    s->BP = gb_mv_create_like(X, s->dt);
+    if (!s->BX || !s->BR || !s->BP) return gb_fail(ctx, "out of device memory");
+  } else {
+    s->BX = s->X;
+    s->BR = s->R;
+    s->BP = s->P;
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------- constraints */
+
+/* BY, YBY = chol(BY'Y)^-1 (lobpcg.c:700-751).  Returns 1 on dependent Y. */
+static int setup_constraints(solver_t* s, gpu_MultiVector* Yuser)
+{
+  gpu_Context* ctx = s->ctx;
+  int info = 0;
+  const int ny = s->ny;
+  /* constraints live in the phase dtype */
+  if (Yuser->dtype == s->dt) {
+    s->Y = Yuser;
+  } else {
+    s->Y = gb_mv_create_like(Yuser, s->dt);
+    if (!s->Y || d_copy(s, Yuser, s->Y)) return -1;
+  }
+  s->BY = s->Y;
+  if (!s->noB) {
+    s->BY = gb_mv_create_like(s->Y, s->dt);
+    if (!s->BY || d_apply(s, s->B, s->Bdata, s->Y, s->BY)) return -1;
+  }
+  if (d_gram(s, s->BY, s->Y, s->gYBY, ny)) return -1;
+  if (gb_cholqr_factor(ctx, s->gYBY, ny, ny, s->info) || read_info(s, &info)) return -1;
+  return info ? 1 : 0;
+}
+
+/* x <- x - Y (YBY^-T YBY^-1 (BY' x)) for the active columns of x; W must
+   carry the same mask as x (lobpcg.c:742-750, 996-1012) */
+static int project_constraints(solver_t* s, gpu_MultiVector* x)
+{
+  const int ny = s->ny, w = x->num_active;
+  if (s->W->num_active != w) return gb_fail(s->ctx, "constraints: W mask mismatch");
+  if (d_gram(s, s->BY, x, s->gYBX, ny)) return -1;
+  if (gb_small_gemm(s->ctx, s->gYBY, ny, 1, s->gYBX, ny, 0, s->tYBX, ny, ny, w, ny)) return -1;
+  if (gb_small_gemm(s->ctx, s->gYBY, ny, 0, s->tYBX, ny, 0, s->gYBX, ny, ny, w, ny)) return -1;
+  if (d_bymat(s, s->Y, s->gYBX, ny, s->W)) return -1;
+  return d_axpy(s, -1.0, s->W, x);
+}
+
+/* --------------------------------------------------------------- phase */
+
+typedef struct {
+  int* iteration;       /* global iteration counter (reference semantics) */
+  int maxit;
+  int it_base;          /* iterations completed before this phase */
+  double* lam_hist;
+  int lam_gh;
+  double* res_hist;
+  int res_gh;
+  int stop_fp32;        /* FP32 phase: hand over to FP64 on these criteria */
+  double fp64_below;
+  int stall_limit;
+  int handed_over;      /* out: the FP32 phase stopped for the hand-over */
+} phase_ctl;
+
+/* the initial B-orthonormalisation + Rayleigh-Ritz of a phase
+   (lobpcg.c:853-962).  Returns the reference exit flag or -2 on CUDA error. */
+static int phase_setup(solver_t* s)
+{
+  const int k = s->k, k3 = s->k3;
+  int info = 0;
+  for (int i = 0; i < k; i++) s->mask[i] = 1;
+  gb_mv_set_mask_host(s->R, s->mask);
+  gb_mv_set_mask_host(s->P, s->mask);
+  gb_mv_set_mask_host(s->AR, s->mask);
+  gb_mv_set_mask_host(s->AP, s->mask);
+  gb_mv_set_mask_host(s->AX, NULL);
+  gb_mv_set_mask_host(s->X, NULL);
+  if (!s->noB) {
+    gb_mv_set_mask_host(s->BR, s->mask);
+    gb_mv_set_mask_host(s->BP, s->mask);
+    gb_mv_set_mask_host(s->BX, NULL);
+  }
+  gb_mv_set_mask_host(s->W, s->mask);
+
+  if (!s->noB && d_apply(s, s->B, s->Bdata, s->X, s->BX)) return -2;
+  if (d_implicit_qr(s, s->X, s->BX, s->gB, k3, s->W, &info)) return -2;
+  if (info) {
+    err_message(s->verbosity, "Bad initial vectors: orthonormalization failed\n");
+    if (s->verbosity) printf("DPOTRF INFO = %d\n", info);
+    return info;
+  }
+  if (!s->noB) {
+    if (d_bymat(s, s->BX, s->gB, k3, s->W) || d_copy(s, s->W, s->BX)) return -2;
+  }
+  if (d_apply(s, s->A, s->Adata, s->X, s->AX)) return -2;
+  if (d_gram(s, s->X, s->AX, s->gA, k3) || gb_small_symmetrize(s->ctx, s->gA, k3, k)) return -2;
+  if (d_gram(s, s->X, s->BX, s->gB, k3) || gb_small_symmetrize(s->ctx, s->gB, k3, k)) return -2;
+  if (d_sygv(s, k, s->lam, &info)) return -2;
+  if (info) {
+    err_message(s->verbosity, "Bad problem: Rayleigh-Ritz in the initial subspace failed\n");
+    if (s->verbosity) printf("DSYGV INFO = %d\n", info);
+    return info;
+  }
+  if (d_bymat(s, s->X, s->gA, k3, s->W) || d_copy(s, s->W, s->X)) return -2;
+  if (d_bymat(s, s->AX, s->gA, k3, s->W) || d_copy(s, s->W, s->AX)) return -2;
+  if (!s->noB && (d_bymat(s, s->BX, s->gA, k3, s->W) || d_copy(s, s->W, s->BX))) return -2;
+  if (d_bydiag_lambda(s, s->BX, NULL, s->R) || d_axpy(s, -1.0, s->AX, s->R)) return -2;
+  if (d_resnorms(s, s->R, NULL) || fetch_lambda(s)) return -2;
+  return 0;
+}
+
+static int nonfinite(const double* v, int k)
+{
+  for (int i = 0; i < k; i++)
+    if (!isfinite(v[i])) return 1;
+  return 0;
+}
+
+/* the main loop of one phase (lobpcg.c:965-1318).  Returns the exit flag
+   (0 or a factorisation INFO) or -2 on a CUDA error; *ctl->iteration
+   follows the reference's counter. */
+static int phase_loop(solver_t* s, phase_ctl* ctl)
+{
+  const int k = s->k, k3 = s->k3;
+  int exitflag = 0, info = 0;
+  int sizeR, sizeP, sizeA, firstR, lastR, firstP;
+  int* it = ctl->iteration;
+  double best = HUGE_VAL;
+  int stall = 0;
+
+  for (*it = ctl->it_base + 1; exitflag == 0 && *it <= ctl->maxit; (*it)++) {
+    /* soft locking (lobpcg.c:265-294) */
+    sizeR = 0;
+    for (int i = 0; i < k; i++) {
+      s->mask[i] = s->h_norm[i] > fabs(s->h_lam[i]) * s->tol.relative + s->tol.absolute + DBL_EPSILON;
+      sizeR += s->mask[i];
+    }
+    if (sizeR < 1) break;
+    if (ctl->stop_fp32) {
+      double mx = 0.0;
+      for (int i = 0; i < k; i++)
+        if (s->mask[i] && s->h_norm[i] > mx) mx = s->h_norm[i];
+      if (mx < ctl->fp64_below) {
+        ctl->handed_over = 1;
+        break;
+      }
+      if (mx < 0.9 * best) {
+        best = mx;
+        stall = 0;
+      } else if (++stall >= ctl->stall_limit) {
+        ctl->handed_over = 1;
+        break;
+      }
+    }
+    gb_mv_set_mask_host(s->R, s->mask);
+    gb_mv_set_mask_host(s->P, s->mask);
+    gb_mv_set_mask_host(s->AR, s->mask);
+    gb_mv_set_mask_host(s->AP, s->mask);
+    if (!s->noB) {
+      gb_mv_set_mask_host(s->BR, s->mask);
+      gb_mv_set_mask_host(s->BP, s->mask);
+    }
+    gb_mv_set_mask_host(s->W, s->mask);
+
+    if (!s->noT) {
+      if (d_apply(s, s->T, s->Tdata, s->R, s->W) || d_copy(s, s->W, s->R)) return -2;
+    }
+    if (!s->noY && project_constraints(s, s->R)) return -2;
+
+    firstR = k;
+    lastR = k + sizeR;
+    firstP = lastR;
+    double* upR = s->gB + firstR + (size_t)firstR * k3;
+    if (!s->noB && d_apply(s, s->B, s->Bdata, s->R, s->BR)) return -2;
+    if (d_implicit_qr(s, s->R, s->BR, upR, k3, s->W, &info)) return -2;
+    exitflag = info;
+    if (exitflag && ctl->stop_fp32) {
+      /* FP32 storage cannot orthonormalise R any more: X is still the
+         previous iteration's block, continue from it in FP64 */
+      ctl->handed_over = 1;
+      exitflag = 0;
+      break;
+    }
+    if (exitflag) {
+      err_message(s->verbosity, "Orthonormalization of residuals failed\n");
+      if (s->verbosity) printf("DPOTRF INFO = %d\n", exitflag);
+      break;
+    }
+    if (!s->noB && (d_bymat(s, s->BR, upR, k3, s->W) || d_copy(s, s->W, s->BR))) return -2;
+    if (d_apply(s, s->A, s->Adata, s->R, s->AR)) return -2;
+
+    if (*it > ctl->it_base + 1) {
+      double* upP = s->gB + firstP + (size_t)firstP * k3;
+      sizeP = sizeR;
+      if (d_implicit_qr(s, s->P, s->BP, upP, k3, s->W, &info)) return -2;
+      exitflag = info;
+      if (exitflag) {
+        sizeP = 0; /* lobpcg.c:1056-1063 */
+      } else {
+        if (!s->noB && (d_bymat(s, s->BP, upP, k3, s->W) || d_copy(s, s->W, s->BP))) return -2;
+        if (d_bymat(s, s->AP, upP, k3, s->W) || d_copy(s, s->W, s->AP)) return -2;
+      }
+    } else {
+      sizeP = 0;
+    }
+    sizeA = lastR + sizeP;
+
+    /* Gram blocks, implicit identities (lobpcg.c:1092-1160) */
+    if (gb_small_diag(s->ctx, s->gA, k3, k, s->lam)) return -2;
+    if (d_gram(s, s->R, s->AX, s->gA + firstR, k3)) return -2;
+    if (d_gram(s, s->R, s->AR, s->gA + firstR + (size_t)firstR * k3, k3)) return -2;
+    if (gb_small_symmetrize(s->ctx, s->gA + firstR + (size_t)firstR * k3, k3, sizeR)) return -2;
+    if (gb_small_identity(s->ctx, s->gB, k3, k, k)) return -2;
+    if (d_gram(s, s->R, s->BX, s->gB + firstR, k3)) return -2;
+    if (gb_small_identity(s->ctx, upR, k3, sizeR, sizeR)) return -2;
+    if (*it > ctl->it_base + 1) {
+      double* aP = s->gA + firstP;
+      if (d_gram(s, s->P, s->AX, aP, k3)) return -2;
+      if (d_gram(s, s->P, s->AR, aP + (size_t)firstR * k3, k3)) return -2;
+      if (d_gram(s, s->P, s->AP, aP + (size_t)firstP * k3, k3)) return -2;
+      if (gb_small_symmetrize(s->ctx, aP + (size_t)firstP * k3, k3, sizeR)) return -2;
+      if (d_gram(s, s->P, s->BX, s->gB + firstP, k3)) return -2;
+      if (d_gram(s, s->P, s->BR, s->gB + firstP + (size_t)firstR * k3, k3)) return -2;
+      if (gb_small_identity(s->ctx, s->gB + firstP + (size_t)firstP * k3, k3, sizeR, sizeR))
+        return -2;
+    }
+
+    /* Rayleigh-Ritz (lobpcg.c:1164-1181) */
+    if (d_sygv(s, sizeA, s->lamAB, &info)) return -2;
+    exitflag = info;
+    if (exitflag != 0 && ctl->stop_fp32) {
+      ctl->handed_over = 1;
+      exitflag = 0;
+      break;
+    }
+    if (exitflag != 0) {
+      err_message(s->verbosity, "GEVP solver failure\n");
+      fprintf(stderr, "Return Code %d\n", exitflag);
+      printf("INFO = %d\n", exitflag);
+      fflush(stdout);
+      (*it)--;
+      break;
+    }
+    if (gb_memcpy_d2d(s->ctx, s->lam, s->lamAB, sizeof(double) * k)) return -2;
+
+    /* P and X updates (lobpcg.c:1191-1272); coordinates are columns 0..k-1
+       of gramA, rows firstR.. for R and firstP.. for P */
+    const double* cX = s->gA;
+    const double* cR = s->gA + firstR;
+    const double* cP = s->gA + firstP;
+    if (*it > ctl->it_base + 1) {
+      gb_mv_set_mask_host(s->W, NULL);
+      if (d_bymat(s, s->P, cP, k3, s->W)) return -2;
+      gb_mv_set_mask_host(s->P, NULL);
+      if (d_copy(s, s->W, s->P)) return -2;
+      if (d_bymat(s, s->AP, cP, k3, s->W)) return -2;
+      gb_mv_set_mask_host(s->AP, NULL);
+      if (d_copy(s, s->W, s->AP)) return -2;
+      if (!s->noB) {
+        if (d_bymat(s, s->BP, cP, k3, s->W)) return -2;
+        gb_mv_set_mask_host(s->BP, NULL);
+        if (d_copy(s, s->W, s->BP)) return -2;
+      }
+      if (d_bymat(s, s->R, cR, k3, s->W) || d_axpy(s, 1.0, s->W, s->P)) return -2;
+      if (d_bymat(s, s->AR, cR, k3, s->W) || d_axpy(s, 1.0, s->W, s->AP)) return -2;
+      if (!s->noB && (d_bymat(s, s->BR, cR, k3, s->W) || d_axpy(s, 1.0, s->W, s->BP))) return -2;
+    } else {
+      gb_mv_set_mask_host(s->P, NULL);
+      if (d_bymat(s, s->R, cR, k3, s->P)) return -2;
+      gb_mv_set_mask_host(s->AP, NULL);
+      if (d_bymat(s, s->AR, cR, k3, s->AP)) return -2;
+      if (!s->noB) {
+        gb_mv_set_mask_host(s->BP, NULL);
+        if (d_bymat(s, s->BR, cR, k3, s->BP)) return -2;
+      }
+    }
+    gb_mv_set_mask_host(s->W, NULL);
+    if (d_copy(s, s->X, s->W) || d_bymat(s, s->W, cX, k3, s->X) || d_axpy(s, 1.0, s->P, s->X))
+      return -2;
+    if (d_copy(s, s->AX, s->W) || d_bymat(s, s->W, cX, k3, s->AX) || d_axpy(s, 1.0, s->AP, s->AX))
+      return -2;
+    if (!s->noB) {
+      if (d_copy(s, s->BX, s->W) || d_bymat(s, s->W, cX, k3, s->BX) ||
+          d_axpy(s, 1.0, s->BP, s->BX))
+        return -2;
+    }
+
+    /* residuals of the active columns (lobpcg.c:1274-1286) */
+    gb_mv_set_mask_host(s->AX, s->mask);
+    gb_mv_set_mask_host(s->BX, s->mask);
+    if (d_bydiag_lambda(s, s->BX, s->mask, s->R) || d_axpy(s, -1.0, s->AX, s->R)) return -2;
+    if (d_resnorms(s, s->R, s->mask) || fetch_lambda(s)) return -2;
+    if (nonfinite(s->h_lam, k)) {
+      gb_fail(s->ctx, "non-finite Ritz values");
+      return -2;
+    }
+
+    {
+      const int col = *it;
+      if (ctl->lam_hist && col <= ctl->maxit)
+        memcpy(ctl->lam_hist + (size_t)col * ctl->lam_gh, s->h_lam, sizeof(double) * k);
+      if (ctl->res_hist && col <= ctl->maxit)
+        memcpy(ctl->res_hist + (size_t)col * ctl->res_gh, s->h_norm, sizeof(double) * k);
+    }
+    if (s->verbosity == 2) {
+      printf("Iteration %d \tbsize %d\n", *it, sizeR);
+      dump_lambda(s->h_norm, s->h_lam, *it, k);
+    } else if (s->verbosity == 1) {
+      printf("Iteration %d \tbsize %d \tmaxres %22.14e\n", *it, sizeR, max_value(s->h_norm, k));
+    }
+
+    gb_mv_set_mask_host(s->AX, NULL);
+    gb_mv_set_mask_host(s->BX, NULL);
+    gb_mv_set_mask_host(s->AP, s->mask);
+    gb_mv_set_mask_host(s->BP, s->mask);
+    gb_mv_set_mask_host(s->P, s->mask);
+    gb_mv_set_mask_host(s->W, s->mask);
+  }
+  return exitflag;
+}
+
+/* ------------------------------------------------------------ the API */
+
+static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_fn B, void* Tdata,
+                     op_fn T, gpu_MultiVector* Yu, lobpcg_Tolerance tol, int maxit, int verbosity,
+                     int* iterationNumber, double* lambda, double* lamHist, int lamGh,
+                     double* resNorms, double* resHist, int resGh)
+{
+  gpu_Context* ctx = Xu->ctx;
+  solver_t s;
+  int exitflag = 0;
+  double t0 = gb_now();
+  long long launches0 = gpu_KernelLaunchCount();
+
+  memset(&s, 0, sizeof(s));
+  memset(&ctx->stats, 0, sizeof(ctx->stats));
+  ctx->err[0] = 0;
+  ctx->potrf_calls = 0;
+  ctx->sygv_calls = 0;
+  s.ctx = ctx;
+  s.n = Xu->size;
+  s.k = Xu->num_vectors;
+  s.k3 = 3 * s.k;
+  s.ny = Yu ? Yu->num_vectors : 0;
+  s.noB = B == NULL;
+  s.noT = T == NULL;
+  s.noY = s.ny == 0;
+  s.A = A;
+  s.B = B;
+  s.T = T;
+  s.Adata = Adata;
+  s.Bdata = Bdata;
+  s.Tdata = Tdata;
+  s.tol = tol;
+  s.verbosity = verbosity;
+  *iterationNumber = 0;
+
+  if (s.k < 1) {
+    err_message(verbosity, "The bloc size is wrong.\n");
+    return WRONG_BLOCK_SIZE;
+  }
+  if (s.k > BLK_MAXCOLS / 3) {
+    gb_fail(ctx, "block size %d exceeds the supported maximum %d", s.k, BLK_MAXCOLS / 3);
+    err_message(verbosity, "The bloc size is wrong.\n");
+    return WRONG_BLOCK_SIZE;
+  }
+  if (Yu && (Yu->size != s.n || s.ny > BLK_MAXCOLS)) {
+    gb_fail(ctx, "constraint block has the wrong shape");
+    return REQUESTED_ACCURACY_NOT_ACHIEVED;
+  }
+
+  /* device small matrices */
+  size_t k3sq = (size_t)s.k3 * s.k3;
+  size_t small = 2 * k3sq + s.k3 + 3 * (size_t)s.k + 3 * (size_t)(s.ny + 1) * (s.ny + s.k + 1) + 16;
+  double* smem = (double*)gb_device_alloc(ctx, sizeof(double) * small);
+  s.info = (int*)gb_device_alloc(ctx, sizeof(int) * 4);
+  s.h_lam = (double*)calloc(s.k, sizeof(double));
+  s.h_norm = (double*)calloc(s.k, sizeof(double));
+  s.mask = (int*)calloc(s.k, sizeof(int));
+  if (!smem || !s.info || !s.h_lam || !s.h_norm || !s.mask) {
+    exitflag = -2;
+    goto done;
+  }
+  cudaMemsetAsync(smem, 0, sizeof(double) * small, (cudaStream_t)ctx->stream);
+  s.gA = smem;
+  s.gB = s.gA + k3sq;
+  s.lamAB = s.gB + k3sq;
+  s.lam = s.lamAB + s.k3;
+  s.norm2 = s.lam + s.k;
+  s.gYBY = s.norm2 + 2 * s.k;
+  s.gYBX = s.gYBY + (size_t)(s.ny + 1) * (s.ny + s.k + 1);
+  s.tYBX = s.gYBX + (size_t)(s.ny + 1) * (s.ny + s.k + 1);
+
+  {
+    const int mixed = ctx->opt.precision == LOBPCG_GPU_MIXED && Xu->dtype == GPU_MV_FLOAT64;
+    gpu_MultiVector* X32 = NULL;
+    phase_ctl ctl;
+    memset(&ctl, 0, sizeof(ctl));
+    ctl.iteration = iterationNumber;
+    ctl.maxit = maxit;
+    ctl.lam_hist = lamHist;
+    ctl.lam_gh = lamGh;
+    ctl.res_hist = resHist;
+    ctl.res_gh = resGh;
+
+    if (verbosity) {
+      printf("\nSolving ");
+      printf(s.noB ? "standard" : "generalized");
+      printf(" eigenvalue problem with");
+      if (s.noT) printf("out");
+      printf(" preconditioning\n\n");
+      printf("block size %d\n\n", s.k);
+      if (s.noY)
+        printf("No constraints\n\n");
+      else if (s.ny > 1)
+        printf("%d constraints\n\n", s.ny);
+      else
+        printf("%d constraint\n\n", s.ny);
+    }
+
+    for (int phase = mixed ? 0 : 1; phase < 2; phase++) {
+      double tp = gb_now();
+      gpu_MultiVector* Xp = Xu;
+      if (phase == 0) {
+        X32 = gb_mv_create_like(Xu, GPU_MV_FLOAT32);
+        if (!X32 || d_copy(&s, Xu, X32)) {
+          exitflag = -2;
+          break;
+        }
+        Xp = X32;
+      } else if (X32) {
+        gb_mv_set_mask_host(X32, NULL);
+        gb_mv_set_mask_host(Xu, NULL);
+        if (d_copy(&s, X32, Xu)) {
+          exitflag = -2;
+          break;
+        }
+      }
+      s.dt = Xp->dtype;
+      if (alloc_blocks(&s, Xp)) {
+        exitflag = -2;
+        break;
+      }
+      if (!s.noY) {
+        int rc = setup_constraints(&s, Yu);
+        if (rc < 0) {
+          exitflag = -2;
+          break;
+        }
+        if (rc > 0) {
+          if (verbosity) printf("Cannot handle linear dependent constraints\n");
+          exitflag = WRONG_CONSTRAINTS;
+          break;
+        }
+        gb_mv_set_mask_host(s.W, NULL);
+        if (project_constraints(&s, s.X)) {
+          exitflag = -2;
+          break;
+        }
+      }
+      exitflag = phase_setup(&s);
+      if (exitflag == 0 && (phase == 1 || !mixed)) {
+        /* the setup of the (last) FP64 phase: record it as iteration 0 when
+           no FP32 iterations ran */
+        if (*iterationNumber == 0) {
+          if (lamHist) memcpy(lamHist, s.h_lam, sizeof(double) * s.k);
+          if (resHist) memcpy(resHist, s.h_norm, sizeof(double) * s.k);
+          if (verbosity == 2)
+            dump_lambda(s.h_norm, s.h_lam, 0, s.k);
+          else if (verbosity == 1)
+            printf("\nInitial Max. Residual %22.14e\n", max_value(s.h_norm, s.k));
+        }
+      } else if (exitflag == 0 && phase == 0) {
+        if (lamHist) memcpy(lamHist, s.h_lam, sizeof(double) * s.k);
+        if (resHist) memcpy(resHist, s.h_norm, sizeof(double) * s.k);
+        if (verbosity == 2)
+          dump_lambda(s.h_norm, s.h_lam, 0, s.k);
+        else if (verbosity == 1)
+          printf("\nInitial Max. Residual %22.14e\n", max_value(s.h_norm, s.k));
+      }
+      if (exitflag == 0) {
+        ctl.it_base = *iterationNumber;
+        ctl.stop_fp32 = phase == 0;
+        ctl.fp64_below = ctx->opt.fp64_below;
+        ctl.stall_limit = ctx->opt.fp32_stall > 0 ? ctx->opt.fp32_stall : 10;
+        ctl.handed_over = 0;
+        exitflag = phase_loop(&s, &ctl);
+        if (phase == 0) {
+          /* the loop counter points one past the last finished iteration */
+          int done_its = *iterationNumber - 1;
+          ctx->stats.iterations_fp32 = done_its;
+          ctx->stats.seconds_fp32 = gb_now() - tp;
+          if (exitflag == 0) {
+            /* hand over to FP64 (also when FP32 met the tolerance: the
+               final residual check is done in FP64) */
+            *iterationNumber = done_its;
+          }
+        } else {
+          ctx->stats.iterations_fp64 = *iterationNumber - 1 - ctl.it_base;
+          ctx->stats.seconds_fp64 = gb_now() - tp;
+        }
+      }
+      if (!s.noY) {
+        if (!s.noB && s.BY != s.Y) gpu_MultiVectorDestroy(s.BY);
+        if (s.Y != Yu) gpu_MultiVectorDestroy(s.Y);
+        s.Y = s.BY = NULL;
+      }
+      free_blocks(&s);
+      if (exitflag != 0) break;
+    }
+    if (X32) {
+      if (exitflag != 0 && exitflag != -2 && *iterationNumber >= 0) {
+        /* failure inside the FP32 phase: return its block */
+        gb_mv_set_mask_host(X32, NULL);
+        gb_mv_set_mask_host(Xu, NULL);
+        d_copy(&s, X32, Xu);
+      }
+      gpu_MultiVectorDestroy(X32);
+    }
+  }
+
+done:
+  if (exitflag == -2) {
+    if (verbosity) fprintf(stderr, "Error in LOBPCG:\n%s\n", ctx->err);
+    exitflag = REQUESTED_ACCURACY_NOT_ACHIEVED;
+  } else if (exitflag == WRONG_CONSTRAINTS) {
+    /* returned as is */
+  } else if (exitflag != 0 || *iterationNumber > maxit) {
+    exitflag = REQUESTED_ACCURACY_NOT_ACHIEVED;
+  }
+  if (exitflag != WRONG_CONSTRAINTS) (*iterationNumber)--;
+  if (*iterationNumber < 0) *iterationNumber = 0;
+  if (s.h_lam) memcpy(lambda, s.h_lam, sizeof(double) * s.k);
+  if (s.h_norm) memcpy(resNorms, s.h_norm, sizeof(double) * s.k);
+  if (verbosity == 1 && exitflag != WRONG_CONSTRAINTS)
+    dump_lambda(s.h_norm, s.h_lam, *iterationNumber, s.k);
+  gb_sync(ctx);
+  gb_device_free(smem);
+  gb_device_free(s.info);
+  free(s.h_lam);
+  free(s.h_norm);
+  free(s.mask);
+  {
+    double mx = 0.0;
+    for (int i = 0; i < s.k; i++)
+      if (resNorms[i] > mx) mx = resNorms[i];
+    ctx->stats.final_max_residual = mx;
+  }
+  ctx->stats.seconds_total = gb_now() - t0;
+  ctx->stats.kernel_launches = gpu_KernelLaunchCount() - launches0;
+  fflush(stdout);
+  return exitflag;
+}
+
+int lobpcg_solve_double(mv_MultiVectorPtr blockVectorX, void* operatorAData,
+                        void (*operatorA)(void*, void*, void*), void* operatorBData,
+                        void (*operatorB)(void*, void*, void*), void* operatorTData,
+                        void (*operatorT)(void*, void*, void*), mv_MultiVectorPtr blockVectorY,
+                        lobpcg_BLASLAPACKFunctions blap_fn, lobpcg_Tolerance tolerance,
+                        int maxIterations, int verbosityLevel, int* iterationNumber,
+                        double* lambda_values, double* lambdaHistory_values,
+                        BlopexInt lambdaHistory_gh, double* residualNorms_values,
+                        double* residualNormsHistory_values, BlopexInt residualNormsHistory_gh)
+{
+  (void)blap_fn;
+  *iterationNumber = 0;
+  if (!blockVectorX || !gb_is_gpu_interpreter(gb_mv_interpreter(blockVectorX))) {
+    if (verbosityLevel)
+      fprintf(stderr,
+              "Error in LOBPCG:\nthe block vector is not a gpu_MultiVector "
+              "(wrap it with the interpreter from GpuSetupInterpreter)\n");
+    return REQUESTED_ACCURACY_NOT_ACHIEVED;
+  }
+  gpu_MultiVector* X = (gpu_MultiVector*)mv_MultiVectorGetData(blockVectorX);
+  gpu_MultiVector* Y = NULL;
+  if (blockVectorY) {
+    if (!gb_is_gpu_interpreter(gb_mv_interpreter(blockVectorY))) {
+      if (verbosityLevel) fprintf(stderr, "Error in LOBPCG:\nconstraints are not a gpu_MultiVector\n");
+      return REQUESTED_ACCURACY_NOT_ACHIEVED;
+    }
+    Y = (gpu_MultiVector*)mv_MultiVectorGetData(blockVectorY);
+    if (Y->num_vectors == 0) Y = NULL;
+  }
+  if (cudaSetDevice(X->ctx->device) != cudaSuccess) return REQUESTED_ACCURACY_NOT_ACHIEVED;
+  return solve_gpu(X, operatorAData, operatorA, operatorBData, operatorB, operatorTData, operatorT, Y,
+                   tolerance, maxIterations, verbosityLevel, iterationNumber, lambda_values,
+                   lambdaHistory_values, lambdaHistory_gh, residualNorms_values,
+                   residualNormsHistory_values, residualNormsHistory_gh);
+}
+
+int lobpcg_solve(mv_MultiVectorPtr blockVectorX, void* operatorAData,
+                 void (*operatorA)(void*, void*, void*), void* operatorBData,
+                 void (*operatorB)(void*, void*, void*), void* operatorTData,
+                 void (*operatorT)(void*, void*, void*), mv_MultiVectorPtr blockVectorY,
+                 lobpcg_BLASLAPACKFunctions blap_fn, lobpcg_Tolerance tolerance, int maxIterations,
+                 int verbosityLevel, int* iterationNumber, void* lambda_values,
+                 void* lambdaHistory_values, BlopexInt lambdaHistory_gh,
+                 double* residualNorms_values, double* residualNormsHistory_values,
+                 BlopexInt residualNormsHistory_gh, lobpcg_Interpreter* lobpcg,
+                 utilities_FortranInterpreter* util)
+{
+  (void)lobpcg;
+  (void)util;
+  return lobpcg_solve_double(blockVectorX, operatorAData, operatorA, operatorBData, operatorB,
+                             operatorTData, operatorT, blockVectorY, blap_fn, tolerance,
+                             maxIterations, verbosityLevel, iterationNumber,
+                             (double*)lambda_values, (double*)lambdaHistory_values,
+                             lambdaHistory_gh, residualNorms_values, residualNormsHistory_values,
+                             residualNormsHistory_gh);
+}

@@ -1,0 +1,589 @@
+// operators.cu -- device operators with the reference callback signature
+// op(void* data, void* X, void* Y), Y(active) = op(X(active)):
+//   CSR SpMM (int32 indices), matrix-free variable-coefficient 7-point (3D)
+//   and 5-point (2D) stencils, the shifted 27-point graph Laplacian, and
+//   diagonal scaling (Jacobi T = D^{-1}, lumped mass B).
+// They replace the serial operators of the reference backend
+// (blopex_serial_double/pcg_multi/pcg_multi.c:167-193 MatMultiVec and
+// blopex_serial_double/matmultivec/matmultivec.c:11-48).
+// FP64 and FP32 multivectors are both accepted; FP32 copies of the
+// coefficients are made on first use.  One thread per row/cell applies the
+// operator to up to 16 columns at once so the coefficients are read once per
+// 16 columns; the x gathers of a warp are coalesced along the row index.
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "internal.h"
+
+enum { OPK_CSR = 1, OPK_ST7 = 2, OPK_ST5 = 3, OPK_ST27 = 4, OPK_DIAG = 5 };
+
+struct gpu_Operator {
+  int kind;
+  gpu_Context* ctx;
+  long n;
+  long nnz;
+  int* rowptr;
+  int* colidx;
+  double* vals;
+  float* vals32;
+  int nx, ny, nz;
+  double shift;
+  double* c[3];   // ST7: cx, cy, cz; ST5: cx, cy
+  float* c32[3];
+  long clen[3];
+  double* w;      // ST27: weights, edge-major [e][cell]
+  float* w32;
+  double* d;      // DIAG
+  float* d32;
+};
+
+static inline cudaStream_t S(gpu_Context* ctx) { return (cudaStream_t)ctx->stream; }
+
+__constant__ int c_st27_off[13][3] = {
+    {1, 0, 0},  {-1, 1, 0}, {0, 1, 0},  {1, 1, 0}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1},
+    {-1, 0, 1}, {0, 0, 1},  {1, 0, 1},  {-1, 1, 1}, {0, 1, 1},  {1, 1, 1}};
+static const int h_st27_off[13][3] = {
+    {1, 0, 0},  {-1, 1, 0}, {0, 1, 0},  {1, 1, 0}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1},
+    {-1, 0, 1}, {0, 0, 1},  {1, 0, 1},  {-1, 1, 1}, {0, 1, 1},  {1, 1, 1}};
+
+#define OP_CB 16
+
+// ---------------------------------------------------------------- CSR
+template <typename T, typename V>
+__global__ void __launch_bounds__(256) csr_kernel(long n, const int* __restrict__ rowptr,
+                                                  const int* __restrict__ colidx,
+                                                  const V* __restrict__ vals, blk_cols X,
+                                                  blk_cols Y, int w)
+{
+  long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int p0 = rowptr[r], p1 = rowptr[r + 1];
+  for (int c0 = 0; c0 < w; c0 += OP_CB) {
+    T acc[OP_CB];
+#pragma unroll
+    for (int b = 0; b < OP_CB; b++) acc[b] = T(0);
+    for (int p = p0; p < p1; p++) {
+      const int ci = colidx[p];
+      const T v = (T)vals[p];
+#pragma unroll
+      for (int b = 0; b < OP_CB; b++)
+        if (c0 + b < w) acc[b] = fma(v, ((const T*)X.col[c0 + b])[ci], acc[b]);
+    }
+#pragma unroll
+    for (int b = 0; b < OP_CB; b++)
+      if (c0 + b < w) ((T*)Y.col[c0 + b])[r] = acc[b];
+  }
+}
+
+// ------------------------------------------------------------ 7-point
+template <typename T>
+__global__ void __launch_bounds__(256) st7_kernel(int nx, int ny, int nz, const T* __restrict__ cx,
+                                                  const T* __restrict__ cy,
+                                                  const T* __restrict__ cz, T shift, blk_cols X,
+                                                  blk_cols Y, int w)
+{
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  long n = (long)nx * ny * nz;
+  if (c >= n) return;
+  const long plane = (long)nx * ny;
+  const int i = (int)(c % nx);
+  const int j = (int)((c / nx) % ny);
+  const int k = (int)(c / plane);
+  const long jk = (long)j + (long)ny * k;
+  const T cw = cx[i + (long)(nx + 1) * jk];
+  const T ce = cx[i + 1 + (long)(nx + 1) * jk];
+  const T cs = cy[i + (long)nx * (j + (long)(ny + 1) * k)];
+  const T cn = cy[i + (long)nx * (j + 1 + (long)(ny + 1) * k)];
+  const T cb = cz[c];
+  const T ct = cz[c + plane];
+  const T dg = cw + ce + cs + cn + cb + ct + shift;
+  for (int col = 0; col < w; col++) {
+    const T* x = (const T*)X.col[col];
+    T v = dg * x[c];
+    if (i > 0) v -= cw * x[c - 1];
+    if (i < nx - 1) v -= ce * x[c + 1];
+    if (j > 0) v -= cs * x[c - nx];
+    if (j < ny - 1) v -= cn * x[c + nx];
+    if (k > 0) v -= cb * x[c - plane];
+    if (k < nz - 1) v -= ct * x[c + plane];
+    ((T*)Y.col[col])[c] = v;
+  }
+}
+
+// ------------------------------------------------------------ 5-point
+template <typename T>
+__global__ void __launch_bounds__(256) st5_kernel(int nx, int ny, const T* __restrict__ cx,
+                                                  const T* __restrict__ cy, T shift, blk_cols X,
+                                                  blk_cols Y, int w)
+{
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  long n = (long)nx * ny;
+  if (c >= n) return;
+  const int i = (int)(c % nx);
+  const int j = (int)(c / nx);
+  const T cw = cx[i + (long)(nx + 1) * j];
+  const T ce = cx[i + 1 + (long)(nx + 1) * j];
+  const T cs = cy[c];
+  const T cn = cy[c + nx];
+  const T dg = cw + ce + cs + cn + shift;
+  for (int col = 0; col < w; col++) {
+    const T* x = (const T*)X.col[col];
+    T v = dg * x[c];
+    if (i > 0) v -= cw * x[c - 1];
+    if (i < nx - 1) v -= ce * x[c + 1];
+    if (j > 0) v -= cs * x[c - nx];
+    if (j < ny - 1) v -= cn * x[c + nx];
+    ((T*)Y.col[col])[c] = v;
+  }
+}
+
+// ----------------------------------------------------------- 27-point
+// weights stored edge-major: w[e*n + cell] for the forward edge e of cell
+template <typename T>
+__global__ void __launch_bounds__(256) st27_kernel(int nx, int ny, int nz, const T* __restrict__ wt,
+                                                   T shift, blk_cols X, blk_cols Y, int w)
+{
+  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long n = (long)nx * ny * nz;
+  if (c >= n) return;
+  const int i = (int)(c % nx);
+  const int j = (int)((c / nx) % ny);
+  const int k = (int)(c / ((long)nx * ny));
+  T we[26];
+  long nb[26];
+  T dg = shift;
+#pragma unroll
+  for (int e = 0; e < 13; e++) {
+    // forward edge (c, c + off_e) and backward edge (c - off_e, c)
+    const int di = c_st27_off[e][0], dj = c_st27_off[e][1], dk = c_st27_off[e][2];
+    const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+    const long off = di + (long)nx * (dj + (long)ny * dk);
+    if (i2 >= 0 && i2 < nx && j2 >= 0 && j2 < ny && k2 >= 0 && k2 < nz) {
+      we[e] = wt[e * n + c];
+      nb[e] = c + off;
+    } else {
+      we[e] = T(0);
+      nb[e] = c;
+    }
+    const int i3 = i - di, j3 = j - dj, k3 = k - dk;
+    if (i3 >= 0 && i3 < nx && j3 >= 0 && j3 < ny && k3 >= 0 && k3 < nz) {
+      we[13 + e] = wt[e * n + c - off];
+      nb[13 + e] = c - off;
+    } else {
+      we[13 + e] = T(0);
+      nb[13 + e] = c;
+    }
+    dg += we[e] + we[13 + e];
+  }
+  for (int col = 0; col < w; col++) {
+    const T* x = (const T*)X.col[col];
+    T v = dg * x[c];
+#pragma unroll
+    for (int e = 0; e < 26; e++) v -= we[e] * x[nb[e]];
+    ((T*)Y.col[col])[c] = v;
+  }
+}
+
+// ----------------------------------------------------------- diagonal
+template <typename T, typename V>
+__global__ void diag_kernel(long n, const V* __restrict__ d, blk_cols X, blk_cols Y)
+{
+  const T* x = (const T*)X.col[blockIdx.y];
+  T* y = (T*)Y.col[blockIdx.y];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    y[r] = (T)d[r] * x[r];
+}
+
+// ------------------------------------------------------------ helpers
+template <typename TI, typename TO>
+__global__ void cast_kernel(const TI* __restrict__ a, TO* __restrict__ b, long n)
+{
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    b[r] = (TO)a[r];
+}
+
+static float* make_f32(gpu_Context* ctx, const double* src, long n)
+{
+  float* dst = (float*)gb_device_alloc(ctx, sizeof(float) * (size_t)(n > 0 ? n : 1));
+  if (!dst) return NULL;
+  unsigned blocks = (unsigned)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  cast_kernel<double, float><<<blocks, 256, 0, S(ctx)>>>(src, dst, n);
+  gb_count_launch(1);
+  if (gb_cuda_check(ctx, (int)cudaGetLastError(), "cast")) {
+    gb_device_free(dst);
+    return NULL;
+  }
+  return dst;
+}
+
+static double* upload(gpu_Context* ctx, const void* host, size_t bytes)
+{
+  double* d = (double*)gb_device_alloc(ctx, bytes);
+  if (!d) return NULL;
+  if (gb_memcpy_h2d(ctx, d, host, bytes)) {
+    gb_device_free(d);
+    return NULL;
+  }
+  return d;
+}
+
+static gpu_Operator* op_new(gpu_Context* ctx, int kind, long n)
+{
+  gpu_Operator* op = (gpu_Operator*)calloc(1, sizeof(gpu_Operator));
+  op->kind = kind;
+  op->ctx = ctx;
+  op->n = n;
+  return op;
+}
+
+extern "C" void gpu_OperatorDestroy(gpu_Operator* op)
+{
+  if (!op) return;
+  cudaStreamSynchronize(S(op->ctx));
+  gb_device_free(op->rowptr);
+  gb_device_free(op->colidx);
+  gb_device_free(op->vals);
+  gb_device_free(op->vals32);
+  for (int a = 0; a < 3; a++) {
+    gb_device_free(op->c[a]);
+    gb_device_free(op->c32[a]);
+  }
+  gb_device_free(op->w);
+  gb_device_free(op->w32);
+  gb_device_free(op->d);
+  gb_device_free(op->d32);
+  free(op);
+}
+
+extern "C" gpu_Operator* gpu_CSRMatrixCreate(gpu_Context* ctx, long n, long nnz, const int* rowptr,
+                                             const int* colidx, const double* vals)
+{
+  if (n <= 0 || nnz < 0) {
+    gb_fail(ctx, "CSR: bad sizes n=%ld nnz=%ld", n, nnz);
+    return NULL;
+  }
+  gpu_Operator* op = op_new(ctx, OPK_CSR, n);
+  op->nnz = nnz;
+  op->rowptr = (int*)upload(ctx, rowptr, sizeof(int) * (size_t)(n + 1));
+  op->colidx = (int*)upload(ctx, colidx, sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+  op->vals = upload(ctx, vals, sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+  if (!op->rowptr || !op->colidx || !op->vals) {
+    gpu_OperatorDestroy(op);
+    return NULL;
+  }
+  return op;
+}
+
+extern "C" gpu_Operator* gpu_Stencil7Create(gpu_Context* ctx, int nx, int ny, int nz,
+                                            const double* cx, const double* cy, const double* cz,
+                                            double shift)
+{
+  if (nx <= 0 || ny <= 0 || nz <= 0) {
+    gb_fail(ctx, "stencil7: bad grid %d x %d x %d", nx, ny, nz);
+    return NULL;
+  }
+  gpu_Operator* op = op_new(ctx, OPK_ST7, (long)nx * ny * nz);
+  op->nx = nx;
+  op->ny = ny;
+  op->nz = nz;
+  op->shift = shift;
+  op->clen[0] = (long)(nx + 1) * ny * nz;
+  op->clen[1] = (long)nx * (ny + 1) * nz;
+  op->clen[2] = (long)nx * ny * (nz + 1);
+  const double* src[3] = {cx, cy, cz};
+  for (int a = 0; a < 3; a++) {
+    op->c[a] = upload(ctx, src[a], sizeof(double) * (size_t)op->clen[a]);
+    if (!op->c[a]) {
+      gpu_OperatorDestroy(op);
+      return NULL;
+    }
+  }
+  return op;
+}
+
+extern "C" gpu_Operator* gpu_Stencil5Create(gpu_Context* ctx, int nx, int ny, const double* cx,
+                                            const double* cy, double shift)
+{
+  if (nx <= 0 || ny <= 0) {
+    gb_fail(ctx, "stencil5: bad grid %d x %d", nx, ny);
+    return NULL;
+  }
+  gpu_Operator* op = op_new(ctx, OPK_ST5, (long)nx * ny);
+  op->nx = nx;
+  op->ny = ny;
+  op->nz = 1;
+  op->shift = shift;
+  op->clen[0] = (long)(nx + 1) * ny;
+  op->clen[1] = (long)nx * (ny + 1);
+  const double* src[2] = {cx, cy};
+  for (int a = 0; a < 2; a++) {
+    op->c[a] = upload(ctx, src[a], sizeof(double) * (size_t)op->clen[a]);
+    if (!op->c[a]) {
+      gpu_OperatorDestroy(op);
+      return NULL;
+    }
+  }
+  return op;
+}
+
+extern "C" gpu_Operator* gpu_Stencil27Create(gpu_Context* ctx, int nx, int ny, int nz,
+                                             const double* w, double shift)
+{
+  if (nx <= 0 || ny <= 0 || nz <= 0) {
+    gb_fail(ctx, "stencil27: bad grid %d x %d x %d", nx, ny, nz);
+    return NULL;
+  }
+  long n = (long)nx * ny * nz;
+  gpu_Operator* op = op_new(ctx, OPK_ST27, n);
+  op->nx = nx;
+  op->ny = ny;
+  op->nz = nz;
+  op->shift = shift;
+  // re-lay the caller's cell-major weights edge-major for coalesced reads
+  double* tmp = (double*)malloc(sizeof(double) * (size_t)n * 13);
+  if (!tmp) {
+    gb_fail(ctx, "stencil27: host allocation failed");
+    free(op);
+    return NULL;
+  }
+  for (long c = 0; c < n; c++)
+    for (int e = 0; e < 13; e++) tmp[(size_t)e * n + c] = w[13 * c + e];
+  op->w = upload(ctx, tmp, sizeof(double) * (size_t)n * 13);
+  free(tmp);
+  if (!op->w) {
+    gpu_OperatorDestroy(op);
+    return NULL;
+  }
+  return op;
+}
+
+extern "C" gpu_Operator* gpu_DiagonalCreate(gpu_Context* ctx, long n, const double* d)
+{
+  if (n <= 0) {
+    gb_fail(ctx, "diagonal: bad size %ld", n);
+    return NULL;
+  }
+  gpu_Operator* op = op_new(ctx, OPK_DIAG, n);
+  op->d = upload(ctx, d, sizeof(double) * (size_t)n);
+  if (!op->d) {
+    gpu_OperatorDestroy(op);
+    return NULL;
+  }
+  return op;
+}
+
+static int ensure_f32(gpu_Operator* op)
+{
+  gpu_Context* ctx = op->ctx;
+  switch (op->kind) {
+    case OPK_CSR:
+      if (!op->vals32 && !(op->vals32 = make_f32(ctx, op->vals, op->nnz))) return -1;
+      break;
+    case OPK_ST7:
+    case OPK_ST5:
+      for (int a = 0; a < (op->kind == OPK_ST7 ? 3 : 2); a++)
+        if (!op->c32[a] && !(op->c32[a] = make_f32(ctx, op->c[a], op->clen[a]))) return -1;
+      break;
+    case OPK_ST27:
+      if (!op->w32 && !(op->w32 = make_f32(ctx, op->w, op->n * 13))) return -1;
+      break;
+    case OPK_DIAG:
+      if (!op->d32 && !(op->d32 = make_f32(ctx, op->d, op->n))) return -1;
+      break;
+  }
+  return 0;
+}
+
+extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
+{
+  gpu_Context* ctx = op->ctx;
+  if (X->size != op->n || Y->size != op->n)
+    return gb_fail(ctx, "operator of size %ld applied to blocks of %ld / %ld rows", op->n,
+                   X->size, Y->size);
+  if (X->num_active != Y->num_active)
+    return gb_fail(ctx, "operator: %d active input columns but %d output columns",
+                   X->num_active, Y->num_active);
+  if (X->dtype != Y->dtype) return gb_fail(ctx, "operator: mixed dtypes");
+  const int w = X->num_active;
+  if (w == 0) return 0;
+  if (w > BLK_MAXCOLS)
+    return gb_fail(ctx, "operator: %d active columns exceed the supported %d", w, BLK_MAXCOLS);
+  blk_cols xc, yc;
+  gb_mv_fill_cols(X, &xc, 0);
+  gb_mv_fill_cols(Y, &yc, 0);
+  const int f32 = X->dtype == GPU_MV_FLOAT32;
+  if (f32 && ensure_f32(op)) return -1;
+  const long n = op->n;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  const double es = f32 ? 4.0 : 8.0;
+  double bytes = 2.0 * es * n * w, flops = 0.0;
+  int cls = GB_K_DIAG;
+  switch (op->kind) {
+    case OPK_CSR:
+      cls = GB_K_CSR;
+      bytes += op->nnz * (es + 4.0) + 4.0 * (n + 1);
+      flops = 2.0 * op->nnz * w;
+      break;
+    case OPK_ST7:
+      cls = GB_K_ST7;
+      bytes += es * (op->clen[0] + op->clen[1] + op->clen[2]);
+      flops = 13.0 * n * w;
+      break;
+    case OPK_ST5:
+      cls = GB_K_ST5;
+      bytes += es * (op->clen[0] + op->clen[1]);
+      flops = 9.0 * n * w;
+      break;
+    case OPK_ST27:
+      cls = GB_K_ST27;
+      bytes += es * 13.0 * n;
+      flops = 53.0 * n * w;
+      break;
+    default:
+      bytes += es * n;
+      flops = 1.0 * n * w;
+  }
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, cls);
+  switch (op->kind) {
+    case OPK_CSR:
+      if (f32)
+        csr_kernel<float, float><<<blocks, 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx, op->vals32,
+                                                             xc, yc, w);
+      else
+        csr_kernel<double, double><<<blocks, 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx,
+                                                               op->vals, xc, yc, w);
+      break;
+    case OPK_ST7:
+      if (f32)
+        st7_kernel<float><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
+                                                      op->c32[2], (float)op->shift, xc, yc, w);
+      else
+        st7_kernel<double><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0], op->c[1],
+                                                       op->c[2], op->shift, xc, yc, w);
+      break;
+    case OPK_ST5:
+      if (f32)
+        st5_kernel<float><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->c32[0], op->c32[1],
+                                                      (float)op->shift, xc, yc, w);
+      else
+        st5_kernel<double><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->c[0], op->c[1],
+                                                       op->shift, xc, yc, w);
+      break;
+    case OPK_ST27:
+      if (f32)
+        st27_kernel<float><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->w32,
+                                                       (float)op->shift, xc, yc, w);
+      else
+        st27_kernel<double><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->w, op->shift,
+                                                        xc, yc, w);
+      break;
+    case OPK_DIAG: {
+      long want = (n + 255) / 256;
+      long cap = (long)ctx->num_sms * 8 / w;
+      if (cap < 4) cap = 4;
+      if (want > cap) want = cap;
+      dim3 grid((unsigned)want, w);
+      if (f32)
+        diag_kernel<float, float><<<grid, 256, 0, S(ctx)>>>(n, op->d32, xc, yc);
+      else
+        diag_kernel<double, double><<<grid, 256, 0, S(ctx)>>>(n, op->d, xc, yc);
+      break;
+    }
+    default:
+      return gb_fail(ctx, "unknown operator kind %d", op->kind);
+  }
+  gb_prof_end(ctx, &pr, bytes, flops);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "operator");
+}
+
+extern "C" void gpu_OperatorApply(void* op, void* X, void* Y)
+{
+  gpu_Operator* o = (gpu_Operator*)op;
+  if (gb_operator_apply(o, (gpu_MultiVector*)X, (gpu_MultiVector*)Y)) {
+    // the callback has no return value: the error stays in the context and
+    // the solver checks it after the call
+  }
+}
+
+// diagonal of the operator, on the host
+__global__ void csr_diag_kernel(long n, const int* rowptr, const int* colidx, const double* vals,
+                                double* out)
+{
+  long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double d = 0.0;
+  for (int p = rowptr[r]; p < rowptr[r + 1]; p++)
+    if (colidx[p] == r) d += vals[p];
+  out[r] = d;
+}
+
+extern "C" int gpu_OperatorDiagonal(gpu_Operator* op, double* host_diag)
+{
+  gpu_Context* ctx = op->ctx;
+  const long n = op->n;
+  if (op->kind == OPK_DIAG) return gb_memcpy_d2h(ctx, host_diag, op->d, sizeof(double) * n);
+  if (op->kind == OPK_CSR) {
+    double* tmp = (double*)gb_device_alloc(ctx, sizeof(double) * n);
+    if (!tmp) return -1;
+    csr_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx,
+                                                                     op->vals, tmp);
+    gb_count_launch(1);
+    int rc = gb_cuda_check(ctx, (int)cudaGetLastError(), "csr_diag");
+    if (!rc) rc = gb_memcpy_d2h(ctx, host_diag, tmp, sizeof(double) * n);
+    gb_device_free(tmp);
+    return rc;
+  }
+  // stencils: apply the operator to unit vectors is wasteful; sum on host
+  if (op->kind == OPK_ST7 || op->kind == OPK_ST5) {
+    int na = op->kind == OPK_ST7 ? 3 : 2;
+    double* h[3] = {NULL, NULL, NULL};
+    int rc = 0;
+    for (int a = 0; a < na && !rc; a++) {
+      h[a] = (double*)malloc(sizeof(double) * op->clen[a]);
+      rc = gb_memcpy_d2h(ctx, h[a], op->c[a], sizeof(double) * op->clen[a]);
+    }
+    if (!rc) {
+      const long nx = op->nx, ny = op->ny, nz = op->nz;
+      for (long k = 0; k < nz; k++)
+        for (long j = 0; j < ny; j++)
+          for (long i = 0; i < nx; i++) {
+            long c = i + nx * (j + ny * k);
+            double s = op->shift + h[0][i + (nx + 1) * (j + ny * k)] +
+                       h[0][i + 1 + (nx + 1) * (j + ny * k)] + h[1][i + nx * (j + (ny + 1) * k)] +
+                       h[1][i + nx * (j + 1 + (ny + 1) * k)];
+            if (na == 3) s += h[2][c] + h[2][c + nx * ny];
+            host_diag[c] = s;
+          }
+    }
+    for (int a = 0; a < na; a++) free(h[a]);
+    return rc;
+  }
+  if (op->kind == OPK_ST27) {
+    double* hw = (double*)malloc(sizeof(double) * n * 13);
+    int rc = gb_memcpy_d2h(ctx, hw, op->w, sizeof(double) * n * 13);
+    if (!rc) {
+      const long nx = op->nx, ny = op->ny, nz = op->nz;
+      for (long c = 0; c < n; c++) host_diag[c] = op->shift;
+      for (long k = 0; k < nz; k++)
+        for (long j = 0; j < ny; j++)
+          for (long i = 0; i < nx; i++) {
+            long c = i + nx * (j + ny * k);
+            for (int e = 0; e < 13; e++) {
+              long i2 = i + h_st27_off[e][0], j2 = j + h_st27_off[e][1], k2 = k + h_st27_off[e][2];
+              if (i2 < 0 || i2 >= nx || j2 < 0 || j2 >= ny || k2 < 0 || k2 >= nz) continue;
+              long d = i2 + nx * (j2 + ny * k2);
+              host_diag[c] += hw[(size_t)e * n + c];
+              host_diag[d] += hw[(size_t)e * n + c];
+            }
+          }
+    }
+    free(hw);
+    return rc;
+  }
+  return gb_fail(ctx, "operator diagonal: unknown kind");
+}

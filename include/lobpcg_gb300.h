@@ -1,0 +1,156 @@
+/*
+ * lobpcg_gb300.h -- the GB300 (sm_103a) backend behind the BLOPEX C API.
+ *
+ * Replaces the serial-double backend of the reference:
+ *   serial_Multi_Vector (blopex_serial_double/multivector/multi_vector.h:22-32)
+ *       -> gpu_MultiVector, a device-resident column-major n x k block;
+ *   SerialSetupInterpreter (blopex_serial_double/pcg_multi/pcg_multi.c:207-242)
+ *       -> GpuSetupInterpreter;
+ *   MatMultiVec / serial_Lapl1DMatMultiVec (pcg_multi.c:167-193,
+ *   matmultivec.c:11-48) -> the device operators below (CSR SpMM, matrix-free
+ *       7-point / 5-point / 27-point stencils, diagonal scaling for Jacobi T
+ *       and lumped-mass B).
+ * No torch or CUDA types appear here: streams are passed as void*
+ * (a cudaStream_t), device memory as void*.
+ */
+#ifndef BLOPEX_GB300_H
+#define BLOPEX_GB300_H
+
+#include "lobpcg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- */
+/* context: device, stream, solver options, statistics               */
+/* ---------------------------------------------------------------- */
+
+typedef struct gpu_Context gpu_Context;
+
+enum { LOBPCG_GPU_FP64 = 0, LOBPCG_GPU_MIXED = 1 };
+enum { GPU_MV_FLOAT64 = 0, GPU_MV_FLOAT32 = 1 };
+
+typedef struct {
+  int precision;            /* LOBPCG_GPU_FP64 (default) or LOBPCG_GPU_MIXED */
+  double compensated_below; /* mixed: hi+lo compensated Gram once max residual < this (1e-6) */
+  double fp64_below;        /* mixed: continue in FP64 once max residual < this (2e-6) */
+  int fp32_stall;           /* mixed: also switch after this many FP32 iterations without
+                               progress of the max residual (10) */
+  int tensor_cores;         /* mixed: 1 = tcgen05 TF32 kernels, 0 = FP32 CUDA-core kernels */
+  int potrf_fail_at;        /* tests: the Nth Cholesky reports INFO = 1 (0 = off) */
+  int sygv_fail_at;         /* tests: the Nth Rayleigh-Ritz solve reports INFO = 1 (0 = off) */
+} lobpcg_gpu_options;
+
+typedef struct {
+  int iterations_fp32;      /* mixed: iterations run in FP32 storage */
+  int iterations_fp64;      /* iterations run in FP64 storage */
+  int iterations_compensated;
+  long long kernel_launches;/* launches of this library's kernels during the last solve */
+  double seconds_total;     /* wall time of the last solve (host clock, synchronised) */
+  double seconds_fp32;
+  double seconds_fp64;
+  double final_max_residual;
+} lobpcg_gpu_stats;
+
+/* per-kernel-class timing, collected with CUDA events on the context's
+   stream when profiling is on (off by default) */
+typedef struct {
+  char name[24];
+  long long launches;
+  double ms;      /* summed event-timed duration */
+  double bytes;   /* summed algorithmic bytes (operands read + results written once) */
+  double flops;   /* summed algorithmic flops */
+} lobpcg_gpu_kernel_time;
+
+/* device < 0: current device.  stream == NULL: the library creates its own
+   non-blocking stream.  Returns NULL on failure. */
+gpu_Context* gpu_ContextCreate(int device, void* stream);
+void gpu_ContextDestroy(gpu_Context* ctx);
+void* gpu_ContextStream(gpu_Context* ctx);
+int gpu_ContextSynchronize(gpu_Context* ctx);
+void gpu_ContextGetOptions(gpu_Context* ctx, lobpcg_gpu_options* opt);
+int gpu_ContextSetOptions(gpu_Context* ctx, const lobpcg_gpu_options* opt);
+void gpu_ContextGetStats(gpu_Context* ctx, lobpcg_gpu_stats* stats);
+/* kernel timers: on/off, read (returns the number of classes written),
+   reset */
+int gpu_ContextSetProfiling(gpu_Context* ctx, int on);
+int gpu_ContextKernelTimes(gpu_Context* ctx, lobpcg_gpu_kernel_time* out, int max);
+void gpu_ContextResetKernelTimes(gpu_Context* ctx);
+/* last error message of this context ("" if none) */
+const char* gpu_ContextLastError(gpu_Context* ctx);
+/* kernels launched by this library since it was loaded (all contexts) */
+long long gpu_KernelLaunchCount(void);
+
+/* ---------------------------------------------------------------- */
+/* device multivector                                                */
+/* ---------------------------------------------------------------- */
+
+typedef struct {
+  void* data;            /* device memory; column j starts at data + j*ld elements */
+  long size;             /* rows n */
+  long ld;               /* leading dimension in elements (>= size, multiple of 32) */
+  BlopexInt num_vectors; /* columns k */
+  BlopexInt dtype;       /* GPU_MV_FLOAT64 or GPU_MV_FLOAT32 */
+  BlopexInt owns_data;
+  BlopexInt num_active;  /* active columns (the mask) */
+  BlopexInt* active;     /* host array: indices of the active columns, ascending */
+  BlopexInt* active_dev; /* device copy of `active` */
+  gpu_Context* ctx;
+} gpu_MultiVector;
+
+gpu_MultiVector* gpu_MultiVectorCreate(gpu_Context* ctx, long n, BlopexInt k, BlopexInt dtype);
+/* wrap caller-owned device memory (not freed by Destroy) */
+gpu_MultiVector* gpu_MultiVectorWrapDevice(gpu_Context* ctx, void* data, long n, long ld,
+                                           BlopexInt k, BlopexInt dtype);
+void gpu_MultiVectorDestroy(gpu_MultiVector* x);
+/* whole-block host transfers, host column-major doubles with leading dimension ldh */
+int gpu_MultiVectorFromHost(gpu_MultiVector* x, const double* host, long ldh);
+int gpu_MultiVectorToHost(gpu_MultiVector* x, double* host, long ldh);
+/* dst(:, all columns) = src(:, all columns), converting FP64 <-> FP32 */
+int gpu_MultiVectorCopy(gpu_MultiVector* src, gpu_MultiVector* dst);
+/* active columns = 2*drand48()-1 after srand48(seed), bit-identical to
+   serial_Multi_VectorSetRandomValues (multi_vector.c:165-184) */
+int gpu_MultiVectorSetRandomValues(gpu_MultiVector* x, BlopexInt seed);
+/* fill `ii` with the device entries (the GPU counterpart of SerialSetupInterpreter) */
+BlopexInt GpuSetupInterpreter(mv_InterfaceInterpreter* ii);
+
+/* ---------------------------------------------------------------- */
+/* operators: callbacks with the reference signature op(data, X, Y)  */
+/* X, Y: gpu_MultiVector*; Y(active) = op(X(active)); FP64 or FP32   */
+/* ---------------------------------------------------------------- */
+
+typedef struct gpu_Operator gpu_Operator;
+
+/* CSR with int32 column indices; host arrays are copied to the device */
+gpu_Operator* gpu_CSRMatrixCreate(gpu_Context* ctx, long n, long nnz, const int* rowptr,
+                                  const int* colidx, const double* vals);
+/* 3D 7-point variable coefficient, Dirichlet: face coefficients
+   cx[(k*ny + j)*(nx+1) + i] for the x-face between cells i-1 and i, likewise
+   cy[(k*(ny+1) + j)*nx + i] and cz[(k*ny + j)*nx + i]; cells i + nx*(j + ny*k);
+   (A x)_c = shift x_c + sum_f c_f (x_c - x_neighbour), x = 0 outside. */
+gpu_Operator* gpu_Stencil7Create(gpu_Context* ctx, int nx, int ny, int nz, const double* cx,
+                                 const double* cy, const double* cz, double shift);
+/* 2D 5-point variable coefficient: cx[j*(nx+1) + i], cy[j*nx + i] */
+gpu_Operator* gpu_Stencil5Create(gpu_Context* ctx, int nx, int ny, const double* cx,
+                                 const double* cy, double shift);
+/* 3D 27-point graph Laplacian + shift: w[13*c + e] is the weight of the edge
+   from cell c to its forward neighbour e (offsets in the order
+   (1,0,0) (-1,1,0) (0,1,0) (1,1,0) (-1,-1,1) (0,-1,1) (1,-1,1) (-1,0,1)
+   (0,0,1) (1,0,1) (-1,1,1) (0,1,1) (1,1,1), as (di,dj,dk)); edges that leave
+   the grid do not exist. */
+gpu_Operator* gpu_Stencil27Create(gpu_Context* ctx, int nx, int ny, int nz, const double* w,
+                                  double shift);
+/* y = d .* x (Jacobi T with d = 1/diag(A); lumped mass B with d = diag(B)) */
+gpu_Operator* gpu_DiagonalCreate(gpu_Context* ctx, long n, const double* d);
+/* diag(A) of an operator, as host doubles (for building Jacobi T) */
+int gpu_OperatorDiagonal(gpu_Operator* op, double* host_diag);
+void gpu_OperatorDestroy(gpu_Operator* op);
+/* the callback to pass as operatorA/B/T together with the gpu_Operator* */
+void gpu_OperatorApply(void* op, void* X, void* Y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

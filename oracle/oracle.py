@@ -39,6 +39,11 @@ def build(ref: bool = True) -> None:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
 
 
+def build_ref_variants() -> None:
+    """FMA-contracted and x87 builds of the reference (x86 only)."""
+    subprocess.run(["make", "-s", "-C", HERE, "ref_variants", f"REF={REF_SRC}"], check=True)
+
+
 def have_ref() -> bool:
     return os.path.exists(REF_SO)
 
@@ -230,15 +235,16 @@ def apply(op: Operator, x: np.ndarray) -> np.ndarray:
 # the unmodified reference (only where the reference checkout was compiled)
 # ---------------------------------------------------------------------------
 
-_ref = None
+_ref = {}
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        if not have_ref():
-            raise RuntimeError("reference harness not built (oracle/_ref missing)")
-        L = ctypes.CDLL(REF_SO)
+def ref_lib(variant: str = ""):
+    """The compiled reference; variant "" (plain -O2), "fma" or "x87"."""
+    if variant not in _ref:
+        path = REF_SO if not variant else REF_SO.replace(".so", f"_{variant}.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"reference harness not built ({path} missing)")
+        L = ctypes.CDLL(path)
         L.ref_set_lapack.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ref_random_block.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.ref_solve.restype = ctypes.c_int
@@ -253,8 +259,8 @@ def ref_lib():
             ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.ref_set_faults.argtypes = [ctypes.c_int, ctypes.c_int]
         L.ref_set_lapack(*lapack_ptrs())
-        _ref = L
-    return _ref
+        _ref[variant] = L
+    return _ref[variant]
 
 
 def ref_random_block(n: int, k: int, seed: int) -> np.ndarray:
@@ -265,9 +271,9 @@ def ref_random_block(n: int, k: int, seed: int) -> np.ndarray:
 
 def ref_solve(n: int, k: int, csr_arrays=None, dense_a=None, b_diag=None, t_diag=None,
               Y=None, seed: int = 0, x0=None, atol=1e-6, rtol=1e-50, maxit=100,
-              verbosity=0, potrf_fail_at=0, sygv_fail_at=0) -> Result:
+              verbosity=0, potrf_fail_at=0, sygv_fail_at=0, variant: str = "") -> Result:
     """Run the reference lobpcg_solve_double with the serial backend."""
-    L = ref_lib()
+    L = ref_lib(variant)
     keep = []
 
     def arr(a, dt):

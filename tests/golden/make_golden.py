@@ -58,6 +58,11 @@ def run_case(name: str) -> dict:
     else:
         kw["dense_a"] = case.dense
     r, text = capture_stdout(lambda: O.ref_solve(case.n, case.k, **kw))
+    variants = {}
+    for v in ("fma", "x87"):
+        rv, _ = capture_stdout(lambda: O.ref_solve(case.n, case.k, variant=v, **kw))
+        variants[v] = {"flag": rv.flag, "iterations": rv.iterations, "lambda": rv.lam.tolist(),
+                       "resnorm": rv.res.tolist()}
     ncol = r.iterations + 1
     out = {
         "name": name,
@@ -69,6 +74,9 @@ def run_case(name: str) -> dict:
         "lambda_hist": r.lam_hist[:, :ncol].T.tolist() if case.k > 0 else [],
         "res_hist": r.res_hist[:, :ncol].T.tolist() if case.k > 0 else [],
         "inputs_sha256": {key: sha(val) for key, val in case.arrays().items()},
+        # the same reference sources built with FMA contraction / x87
+        # arithmetic: the reference's own sensitivity to rounding
+        "variants": variants,
     }
     if case.verbosity:
         out["stdout"] = text
@@ -80,6 +88,7 @@ def run_case(name: str) -> dict:
 def main():
     if not O.have_ref():
         O.build(ref=True)
+    O.build_ref_variants()
     for name in C.NAMES:
         g = run_case(name)
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:

@@ -1,0 +1,43 @@
+"""The parity bar against the golden fixtures.
+
+Each fixture holds the unmodified reference run three ways: the plain -O2
+build (the golden), an FMA-contracted build (gcc's default on arm64 hosts)
+and an x87 build.  Where those agree, the bar is the strict one -- same exit
+flag, iteration count within 2, eigenvalues to 1e-10 relative.  Where the
+reference's own runs spread (rounding-chaotic cases: unconverged or
+degenerate clusters, non-invariant constraints, exactly singular blocks),
+the bar is that envelope: the exit flag of one of the runs, the iteration
+count within the runs' range widened by 2 + the spread, and eigenvalues
+within max(1e-10, 3 x the runs' spread) of the matching run.
+"""
+import numpy as np
+
+LAMBDA_RTOL = 1e-10
+
+
+def runs(g):
+    out = [{"flag": g["flag"], "iterations": g["iterations"], "lambda": g["lambda"]}]
+    out += list(g.get("variants", {}).values())
+    return out
+
+
+def check(g, flag, iterations, lam):
+    """Assert that (flag, iterations, lam) lies inside the reference envelope."""
+    rs = runs(g)
+    same = [r for r in rs if r["flag"] == flag]
+    assert same, f"exit flag {flag} not among the reference runs {[r['flag'] for r in rs]}"
+    its = [r["iterations"] for r in same]
+    spread = max(its) - min(its)
+    lo, hi = min(its) - 2 - spread, max(its) + 2 + spread
+    assert lo <= iterations <= hi, f"iterations {iterations} outside [{lo}, {hi}] ({its})"
+    if iterations == 0 and flag != 0:
+        return
+    lams = np.array([r["lambda"] for r in same])
+    ref = lams[0]
+    scale = np.maximum(np.abs(ref), 1e-300)
+    lspread = float(np.max(np.abs(lams - ref) / scale)) if len(lams) > 1 else 0.0
+    tol = max(LAMBDA_RTOL, 3.0 * lspread)
+    err = np.abs(np.asarray(lam) - lams) / scale
+    best = float(np.min(np.max(err, axis=1)))
+    assert best <= tol, f"eigenvalues differ by {best:.3e} relative (bar {tol:.3e})"
+    return best, tol

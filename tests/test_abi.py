@@ -1,0 +1,59 @@
+"""CPU checks of the C ABI: the library loads and exports every entry point
+declared in include/*.h; the host-only small-matrix routines work.  No GPU
+calls are made here."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+
+from blopex_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for path in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+        src = re.sub(r"typedef\s+struct\s*\{.*?\}\s*\w+\s*;", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w \*]*?\b(\w+)\s*\([^;{]*\)\s*;", src, re.M | re.S):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    declared = declared_functions()
+    assert len(declared) >= 70
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    assert declared <= set(_lib.SIGNATURES), declared - set(_lib.SIGNATURES)
+
+
+def test_library_is_built_for_sm103a():
+    # the build recipe targets exactly one architecture
+    from blopex_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_fortran_matrix_host_routines():
+    lib = _lib.load()
+    m = lib.utilities_FortranMatrixCreate()
+    lib.utilities_FortranMatrixAllocateData(4, 4, m)
+    vals = ctypes.cast(lib.utilities_FortranMatrixValues(m), ctypes.POINTER(ctypes.c_double))
+    rng = np.random.default_rng(0)
+    u = np.triu(rng.uniform(1, 2, (4, 4)))
+    for j in range(4):
+        for i in range(4):
+            vals[i + 4 * j] = u[i, j]
+    lib.utilities_FortranMatrixUpperInv(m)
+    inv = np.array([[vals[i + 4 * j] for j in range(4)] for i in range(4)])
+    np.testing.assert_allclose(np.triu(inv) @ u, np.eye(4), atol=1e-14)
+    assert lib.utilities_FortranMatrixGlobalHeight(m) == 4
+    blk = lib.utilities_FortranMatrixCreate()
+    lib.utilities_FortranMatrixSelectBlock(m, 2, 3, 2, 4, blk)
+    assert lib.utilities_FortranMatrixHeight(blk) == 2 and lib.utilities_FortranMatrixWidth(blk) == 3
+    lib.utilities_FortranMatrixDestroy(blk)
+    lib.utilities_FortranMatrixDestroy(m)

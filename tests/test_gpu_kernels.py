@@ -1,0 +1,113 @@
+"""Device kernels through the C ABI against the oracle / numpy (FP64 and FP32)."""
+import numpy as np
+import pytest
+
+from blopex_gb300 import problems as P
+from blopex_gb300 import solver as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = S.Context(0)
+    yield c
+    c.close()
+
+
+def test_drand48_device_bit_exact(ctx):
+    for n, k, seed in ((40, 5, 1), (8000, 10, 0), (1003, 7, 12345)):
+        X = S.MultiVector(ctx, n, k)
+        X.set_random(seed)
+        assert np.array_equal(X.to_host(), P.drand48_block(n, k, seed))
+
+
+@pytest.mark.parametrize("dtype,rtol", [(S.FLOAT64, 1e-13), (S.FLOAT32, 2e-5)])
+@pytest.mark.parametrize("n,h,w", [(1, 1, 1), (37, 3, 5), (4099, 17, 33), (20000, 96, 64)])
+def test_gram_matches_numpy(ctx, dtype, rtol, n, h, w):
+    rng = np.random.default_rng(n + h + w)
+    x = rng.standard_normal((n, h))
+    y = rng.standard_normal((n, w))
+    if dtype == S.FLOAT32:
+        x, y = x.astype(np.float32).astype(np.float64), y.astype(np.float32).astype(np.float64)
+    X = S.MultiVector.from_host(ctx, x, dtype)
+    Yv = S.MultiVector.from_host(ctx, y, dtype)
+    interp = S._Interp(ctx.lib)
+    xx = ctx.lib.mv_MultiVectorWrap(interp.ptr, X.handle, 0)
+    yy = ctx.lib.mv_MultiVectorWrap(interp.ptr, Yv.handle, 0)
+    gh = h + 3
+    v = np.full((gh, w), 7.0, order="F")
+    ctx.lib.mv_MultiVectorByMultiVector(xx, yy, gh, h, w, v.ctypes.data)
+    ref = x.T @ y
+    scale = np.sqrt(np.outer((x * x).sum(0), (y * y).sum(0)))
+    assert np.all(np.abs(v[:h] - ref) <= rtol * scale + 1e-300)
+    assert np.all(v[h:] == 7.0)
+    ctx.lib.mv_MultiVectorDestroy(xx)
+    ctx.lib.mv_MultiVectorDestroy(yy)
+
+
+@pytest.mark.parametrize("dtype,rtol", [(S.FLOAT64, 1e-13), (S.FLOAT32, 2e-5)])
+@pytest.mark.parametrize("n,h,w", [(5, 1, 1), (1000, 10, 10), (70001, 40, 33)])
+def test_bymatrix_matches_numpy(ctx, dtype, rtol, n, h, w):
+    rng = np.random.default_rng(3 * n + h)
+    x = rng.standard_normal((n, h))
+    c = rng.standard_normal((h + 2, w))
+    if dtype == S.FLOAT32:
+        x = x.astype(np.float32).astype(np.float64)
+    X = S.MultiVector.from_host(ctx, x, dtype)
+    Yv = S.MultiVector(ctx, n, w, dtype)
+    interp = S._Interp(ctx.lib)
+    xx = ctx.lib.mv_MultiVectorWrap(interp.ptr, X.handle, 0)
+    yy = ctx.lib.mv_MultiVectorWrap(interp.ptr, Yv.handle, 0)
+    cf = np.asfortranarray(c)
+    ctx.lib.mv_MultiVectorByMatrix(xx, h + 2, h, w, cf.ctypes.data, yy)
+    ref = x @ c[:h]
+    scale = np.abs(x) @ np.abs(c[:h])
+    assert np.all(np.abs(Yv.to_host() - ref) <= rtol * scale + 1e-300)
+    ctx.lib.mv_MultiVectorDestroy(xx)
+    ctx.lib.mv_MultiVectorDestroy(yy)
+
+
+def _ops(ctx):
+    rng = np.random.default_rng(7)
+    out = []
+    rp, ci, va = P.laplacian3d_csr(9, 7, 5)
+    out.append((S.CSRMatrix(ctx, rp, ci, va), O.csr(rp, ci, va), 315))
+    cx, cy, cz = P.stencil7_coefficients(11, 6, 5, seed=2)
+    out.append((S.Stencil7(ctx, cx, cy, cz, 0.3), O.stencil7(11, 6, 5, cx, cy, cz, 0.3), 330))
+    c = np.exp(rng.standard_normal((13, 17)))
+    sx, sy = P.stencil5_from_cells(c)
+    out.append((S.Stencil5(ctx, sx, sy, 0.1), O.stencil5(17, 13, sx, sy, 0.1), 221))
+    w = P.stencil27_weights(6, 5, 7, seed=4)
+    out.append((S.Stencil27(ctx, 6, 5, 7, w, 0.5), O.stencil27(6, 5, 7, w, 0.5), 210))
+    d = rng.uniform(0.5, 1.5, 333)
+    out.append((S.Diagonal(ctx, d), O.diag(d), 333))
+    return out
+
+
+@pytest.mark.parametrize("dtype,rtol", [(S.FLOAT64, 1e-13), (S.FLOAT32, 3e-6)])
+def test_operators_match_oracle(ctx, dtype, rtol):
+    rng = np.random.default_rng(11)
+    for gop, oop, n in _ops(ctx):
+        for k in (1, 3, 17):
+            x = rng.standard_normal((n, k))
+            if dtype == S.FLOAT32:
+                x = x.astype(np.float32).astype(np.float64)
+            X = S.MultiVector.from_host(ctx, x, dtype)
+            Yv = S.MultiVector(ctx, n, k, dtype)
+            gop.apply(X, Yv)
+            ref = O.apply(oop, x)
+            scale = O.apply(oop, np.abs(x)) if oop.kind == O.OP_DIAG else np.abs(ref).max()
+            np.testing.assert_allclose(Yv.to_host(), ref, rtol=0, atol=rtol * np.max(scale) * 10)
+
+
+def test_operator_diagonal(ctx):
+    for gop, oop, n in _ops(ctx):
+        e = np.zeros(n)
+        d = np.empty(n)
+        for i in range(n):
+            e[:] = 0
+            e[i] = 1
+            d[i] = O.apply(oop, e)[i, 0]
+        np.testing.assert_allclose(gop.diagonal(), d, rtol=1e-13, atol=1e-13)
