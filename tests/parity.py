@@ -36,7 +36,8 @@ def check(g, flag, iterations, lam):
             return
         its = [iterations]
     else:
-        spread = max(its) - min(its)
+        its = [r["iterations"] for r in same]
+    spread = max(its) - min(its)
     lo, hi = min(its) - 2 - spread, max(its) + 2 + spread
     assert lo <= iterations <= hi, f"iterations {iterations} outside [{lo}, {hi}] ({its})"
     if iterations == 0 and flag != 0:
