@@ -142,6 +142,8 @@ SIGNATURES = {
     "gpu_OperatorDiagonal": (c_int, [c_void_p, c_void_p]),
     "gpu_OperatorDestroy": (None, [c_void_p]),
     "gpu_OperatorApply": (None, [c_void_p, c_void_p, c_void_p]),
+    "gpu_GramNoAlloc": (c_int, [c_int, c_long, c_void_p, c_long, c_int, c_void_p, c_long, c_int,
+                                c_void_p, c_int, c_void_p]),
 }
 
 _lib = None

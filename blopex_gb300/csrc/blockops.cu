@@ -505,3 +505,80 @@ extern "C" int gb_drand48_fill(gpu_Context* ctx, int dtype, void* data, long n, 
   gb_count_launch(1);
   return CUDA_LAUNCH_CHECK(ctx, "drand48_fill");
 }
+
+// ------------------------------------------------------------------------
+// Gram product that allocates nothing (gpu_GramNoAlloc in lobpcg_gb300.h).
+// The split-k partial sums live in this file-scope device array instead of
+// the context's cudaMalloc'ed workspace.  Host code must not pass the
+// array's name to a kernel (on the host it is only a stand-in symbol); its
+// device address is looked up once per device with cudaGetSymbolAddress.
+// ------------------------------------------------------------------------
+#define GRAM_NOALLOC_SCRATCH_DOUBLES (512 * 1024) /* 4 MiB per device */
+static __device__ __align__(256) double g_gram_noalloc_scratch[GRAM_NOALLOC_SCRATCH_DOUBLES];
+
+#define GRAM_NOALLOC_MAX_DEVICES 64
+static double* g_noalloc_addr[GRAM_NOALLOC_MAX_DEVICES];
+
+static double* noalloc_scratch(int device)
+{
+  if (device < 0 || device >= GRAM_NOALLOC_MAX_DEVICES) return NULL;
+  if (!g_noalloc_addr[device]) {
+    void* p = NULL;
+    // the caller's device is current here (cudaGetDevice above)
+    if (cudaGetSymbolAddress(&p, g_gram_noalloc_scratch) != cudaSuccess || !p) return NULL;
+    g_noalloc_addr[device] = (double*)p;
+  }
+  return g_noalloc_addr[device];
+}
+
+template <typename T, int TM, int TN>
+static int gram_noalloc_launch(long n, const blk_cols* X, int h, const blk_cols* Y, int w,
+                               double* G, int ldg, double* partial, cudaStream_t stream, int sms)
+{
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  int gx = (h + BM - 1) / BM, gy = (w + BN - 1) / BN;
+  long splits = 2L * sms / (gx * gy);
+  long cap = GRAM_NOALLOC_SCRATCH_DOUBLES / ((long)h * w);  // splits that fit the array
+  if (splits > cap) splits = cap;
+  long max_splits = (n + 255) / 256;
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  long rows = (n + splits - 1) / splits;
+  rows = (rows + 31) / 32 * 32;
+  splits = (n + rows - 1) / rows;
+  if (splits < 1) splits = 1;
+  dim3 grid(gx, gy, (unsigned)splits);
+  // every partial element of the used splits is written before the
+  // reduction reads it, so stale contents from an earlier call never leak
+  gram_partial_kernel<T, TM, TN><<<grid, 256, 0, stream>>>(*X, h, *Y, w, n, rows, partial);
+  gram_reduce_kernel<<<(h * w + 255) / 256, 256, 0, stream>>>(partial, (int)splits, h, w, G, ldg);
+  gb_count_launch(2);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+extern "C" int gpu_GramNoAlloc(int dtype, long n, const void* X, long ldx, int h, const void* Y,
+                               long ldy, int w, double* G, int ldg, void* stream)
+{
+  if (n <= 0 || h <= 0 || w <= 0 || !X || !Y || !G || ldx < n || ldy < n || ldg < h ||
+      (dtype != GPU_MV_FLOAT64 && dtype != GPU_MV_FLOAT32))
+    return -1;
+  if (h > BLK_MAXCOLS || w > BLK_MAXCOLS || (long)h * w > GRAM_NOALLOC_SCRATCH_DOUBLES) return -2;
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess) return -3;
+  double* partial = noalloc_scratch(device);
+  if (!partial) return -3;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
+    sms = 152;
+  const size_t es = dtype == GPU_MV_FLOAT64 ? 8 : 4;
+  blk_cols xc, yc;
+  for (int c = 0; c < h; c++) xc.col[c] = (const char*)X + es * (size_t)ldx * c;
+  for (int c = 0; c < w; c++) yc.col[c] = (const char*)Y + es * (size_t)ldy * c;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == GPU_MV_FLOAT64) {
+    if (h <= 32 && w <= 32) return gram_noalloc_launch<double, 2, 2>(n, &xc, h, &yc, w, G, ldg, partial, s, sms);
+    return gram_noalloc_launch<double, 4, 4>(n, &xc, h, &yc, w, G, ldg, partial, s, sms);
+  }
+  if (h <= 32 && w <= 32) return gram_noalloc_launch<float, 2, 2>(n, &xc, h, &yc, w, G, ldg, partial, s, sms);
+  return gram_noalloc_launch<float, 4, 4>(n, &xc, h, &yc, w, G, ldg, partial, s, sms);
+}

@@ -149,6 +149,41 @@ void gpu_OperatorDestroy(gpu_Operator* op);
 /* the callback to pass as operatorA/B/T together with the gpu_Operator* */
 void gpu_OperatorApply(void* op, void* X, void* Y);
 
+/* ---------------------------------------------------------------- */
+/* Gram product without any allocation                               */
+/* ---------------------------------------------------------------- */
+
+/*
+ * G(0:h, 0:w) = X(:, 0:h)' * Y(:, 0:w) for column-major device blocks X
+ * (leading dimension ldx) and Y (ldy) of n rows, both FP64 (dtype
+ * GPU_MV_FLOAT64) or both FP32 (GPU_MV_FLOAT32); G is FP64 device memory with
+ * leading dimension ldg; the kernels run on `stream` (a cudaStream_t).
+ *
+ * This entry point has no counterpart in the reference.  It is the same
+ * split-k Gram kernel as the solver's (and as mv_MultiVectorByMultiVector
+ * through the GPU interpreter), for callers that cannot allocate device
+ * memory on this path: code running inside another framework's memory
+ * pool that forbids raw cudaMalloc, or latency-critical code that must not
+ * trigger the device synchronisation cudaMalloc/cudaFree can cause.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine; the split-k
+ * partial sums go to one fixed device array of GPU_GRAM_NOALLOC_MAX_DOUBLES
+ * doubles (4 MiB) that every GPU which loads the library holds until exit.
+ *   - h * w must not exceed that maximum and h, w must not exceed 384; larger
+ *     sizes are rejected with return value -2 (nothing is launched).
+ *   - The first call on a device looks the array's address up
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU (concurrent
+ *     streams, or several host threads) race on it and must be serialised
+ *     by the caller.  The array keeps the last call's partial sums; every
+ *     call overwrites all partials it reads, so nothing needs clearing.
+ * Returns 0 on success, -1 for bad arguments, -2 for sizes beyond the
+ * maximum, -3 for a CUDA error.
+ */
+#define GPU_GRAM_NOALLOC_MAX_DOUBLES (512 * 1024)
+int gpu_GramNoAlloc(int dtype, long n, const void* X, long ldx, int h, const void* Y, long ldy,
+                    int w, double* G, int ldg, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
