@@ -27,7 +27,7 @@ class BlasLapack(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("compensated_below", c_double), ("fp64_below", c_double),
                 ("fp32_stall", c_int), ("tensor_cores", c_int), ("potrf_fail_at", c_int),
-                ("sygv_fail_at", c_int)]
+                ("sygv_fail_at", c_int), ("rr_fp64_only", c_int)]
 
 
 class Stats(ctypes.Structure):

@@ -139,8 +139,11 @@ extern "C" int gb_cholqr_factor(gpu_Context* ctx, double* A, int ld, int m, int*
 
 __global__ void __launch_bounds__(DENSE_THREADS) sygv_kernel(double* A, double* B, int ld, int m,
                                                              double* w, int* info, double* C,
-                                                             double* V, int force_fail)
+                                                             double* V, int force_fail,
+                                                             const int* gate)
 {
+  // gate: status word of the fast path; this solver runs only when it failed
+  if (gate && *gate == 0) return;
   __shared__ double s_c[256], s_s[256];
   __shared__ int s_p[256], s_q[256];
   __shared__ int s_done;
@@ -318,18 +321,19 @@ __global__ void __launch_bounds__(DENSE_THREADS) sygv_kernel(double* A, double* 
   if (tid == 0) *info = 0;
 }
 
-extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w, int* info)
+/* One-CTA FP64 solver: used for orders the fast path does not take, when
+   the fast path's FP32 stage fails (gate != NULL: runs only if *gate != 0),
+   and for injected failures (force). */
+extern "C" int gb_sygv_fp64(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w,
+                            int* info, const int* gate, int force)
 {
   if (m > 512) return gb_fail(ctx, "sygv: order %d exceeds 512", m);
   double* scratch = (double*)gb_workspace(ctx, sizeof(double) * (size_t)2 * m * m + 64);
   if (!scratch) return -1;
-  int force = 0;
-  ctx->sygv_calls++;
-  if (ctx->opt.sygv_fail_at > 0 && ctx->sygv_calls == ctx->opt.sygv_fail_at) force = 1;
   gb_prof_rec pr;
   gb_prof_begin(ctx, &pr, GB_K_SYGV);
   sygv_kernel<<<1, DENSE_THREADS, 0, S(ctx)>>>(A, B, ld, m, w, info, scratch,
-                                               scratch + (size_t)m * m, force);
+                                               scratch + (size_t)m * m, force, gate);
   gb_prof_end(ctx, &pr, 32.0 * m * m, 0.0);
   gb_count_launch(1);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "sygv");

@@ -40,6 +40,8 @@ typedef struct {
   int tensor_cores;         /* mixed: 1 = tcgen05 TF32 kernels, 0 = FP32 CUDA-core kernels */
   int potrf_fail_at;        /* tests: the Nth Cholesky reports INFO = 1 (0 = off) */
   int sygv_fail_at;         /* tests: the Nth Rayleigh-Ritz solve reports INFO = 1 (0 = off) */
+  int rr_fp64_only;         /* 1: Rayleigh-Ritz by the one-CTA FP64 Jacobi solver only (default 0:
+                               FP32 Jacobi + FP64 refinement, FP64 Jacobi as fallback) */
 } lobpcg_gpu_options;
 
 typedef struct {
