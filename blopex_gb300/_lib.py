@@ -34,7 +34,9 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations_fp32", c_int), ("iterations_fp64", c_int),
                 ("iterations_compensated", c_int), ("kernel_launches", c_longlong),
                 ("seconds_total", c_double), ("seconds_fp32", c_double),
-                ("seconds_fp64", c_double), ("final_max_residual", c_double)]
+                ("seconds_fp64", c_double), ("final_max_residual", c_double),
+                ("rr_calls", c_int), ("rr_jacobi32_sweeps", c_int), ("rr_max_cluster", c_int),
+                ("rr_fallbacks", c_int)]
 
 
 class KernelTime(ctypes.Structure):
@@ -142,6 +144,8 @@ SIGNATURES = {
     "gpu_OperatorDiagonal": (c_int, [c_void_p, c_void_p]),
     "gpu_OperatorDestroy": (None, [c_void_p]),
     "gpu_OperatorApply": (None, [c_void_p, c_void_p, c_void_p]),
+    "gpu_ExplicitGram": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_int, c_void_p, c_void_p, c_int]),
     "gpu_GramNoAlloc": (c_int, [c_int, c_long, c_void_p, c_long, c_int, c_void_p, c_long, c_int,
                                 c_void_p, c_int, c_void_p]),
 }

@@ -13,7 +13,8 @@ static long long g_launches = 0;
 static const char* k_names[GB_K_COUNT] = {"gram", "xc_update", "spmm_csr", "stencil7",
                                           "stencil5", "stencil27", "diag_scale", "residual",
                                           "blas1", "cholqr", "sygv", "small_dense", "tc_gram",
-                                          "tc_xc_update"};
+                                          "tc_xc_update", "sygv_fp64_gate", "rr_chol64",
+                                          "rr_trsm64", "rr_jacobi32", "rr_gemm64", "rr_refine"};
 
 
 extern "C" void gb_count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
@@ -53,7 +54,7 @@ static void default_options(lobpcg_gpu_options* o)
   o->precision = LOBPCG_GPU_FP64;
   o->compensated_below = 1e-6;
   o->fp64_below = 2e-6;
-  o->fp32_stall = 10;
+  o->fp32_stall = 20;
   o->tensor_cores = 1;
 }
 
@@ -87,6 +88,12 @@ extern "C" gpu_Context* gpu_ContextCreate(int device, void* stream)
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (ctx->num_sms <= 0) ctx->num_sms = 152;
   for (int c = 0; c < GB_K_COUNT; c++) strncpy(ctx->prof[c].name, k_names[c], sizeof(ctx->prof[c].name) - 1);
+  if (cudaMalloc((void**)&ctx->dcount, 8 * sizeof(int)) != cudaSuccess ||
+      cudaMemsetAsync(ctx->dcount, 0, 8 * sizeof(int), (cudaStream_t)ctx->stream) != cudaSuccess) {
+    if (ctx->owns_stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
+    free(ctx);
+    return NULL;
+  }
   return ctx;
 }
 
@@ -189,6 +196,7 @@ extern "C" void gpu_ContextDestroy(gpu_Context* ctx)
   free(ctx->prof_pool);
   free(ctx->prof_pending);
   if (ctx->work) cudaFree(ctx->work);
+  if (ctx->dcount) cudaFree(ctx->dcount);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->owns_stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
   free(ctx);

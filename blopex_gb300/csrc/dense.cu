@@ -140,10 +140,13 @@ extern "C" int gb_cholqr_factor(gpu_Context* ctx, double* A, int ld, int m, int*
 __global__ void __launch_bounds__(DENSE_THREADS) sygv_kernel(double* A, double* B, int ld, int m,
                                                              double* w, int* info, double* C,
                                                              double* V, int force_fail,
-                                                             const int* gate)
+                                                             const int* gate, int* count)
 {
-  // gate: status word of the fast path; this solver runs only when it failed
-  if (gate && *gate == 0) return;
+  // gate: status word of the fast path; this solver runs only when the fast
+  // path failed for a reason it can fix (5 = B not positive definite, which
+  // the fast path has already reported through *info)
+  if (gate && (*gate == 0 || *gate == 5)) return;
+  if (gate && threadIdx.x == 0) atomicAdd(&count[2], 1);
   __shared__ double s_c[256], s_s[256];
   __shared__ int s_p[256], s_q[256];
   __shared__ int s_done;
@@ -331,9 +334,10 @@ extern "C" int gb_sygv_fp64(gpu_Context* ctx, double* A, double* B, int ld, int 
   double* scratch = (double*)gb_workspace(ctx, sizeof(double) * (size_t)2 * m * m + 64);
   if (!scratch) return -1;
   gb_prof_rec pr;
-  gb_prof_begin(ctx, &pr, GB_K_SYGV);
+  gb_prof_begin(ctx, &pr, gate ? GB_K_SYGV_FALLBACK : GB_K_SYGV);
   sygv_kernel<<<1, DENSE_THREADS, 0, S(ctx)>>>(A, B, ld, m, w, info, scratch,
-                                               scratch + (size_t)m * m, force, gate);
+                                               scratch + (size_t)m * m, force, gate,
+                                               ctx->dcount);
   gb_prof_end(ctx, &pr, 32.0 * m * m, 0.0);
   gb_count_launch(1);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "sygv");
@@ -420,4 +424,67 @@ extern "C" int gb_small_gemm(gpu_Context* ctx, const double* A, int lda, int ta,
   small_gemm_kernel<<<small_blocks(h * w), 256, 0, S(ctx)>>>(A, lda, ta, B, ldb, tb, C, ldc, h, w, l);
   gb_count_launch(1);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "small_gemm");
+}
+
+// ---------------------------------------------------------------------------
+// explicit-Gram Rayleigh-Ritz helpers (FP32 phase of the mixed mode)
+// ---------------------------------------------------------------------------
+// d_i = 1/sqrt(H_ii) (1 when H_ii <= 0); Gs = D sym(G) D, Hs = D sym(H) D
+__global__ void scale_pencil_kernel(const double* G, const double* H, double* Gs, double* Hs,
+                                    double* d, int ld, int m)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    double h = H[i + (size_t)i * ld];
+    d[i] = h > 0.0 ? 1.0 / sqrt(h) : 1.0;
+  }
+  __syncthreads();  // single block launch below
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    int i = e % m, j = e / m;
+    double di = d[i], dj = d[j];
+    double g = 0.5 * (G[i + (size_t)j * ld] + G[j + (size_t)i * ld]);
+    double hh = 0.5 * (H[i + (size_t)j * ld] + H[j + (size_t)i * ld]);
+    Gs[i + (size_t)j * ld] = di * g * dj;
+    Hs[i + (size_t)j * ld] = (i == j) ? 1.0 : di * hh * dj;
+  }
+}
+
+extern "C" int gb_scale_pencil(gpu_Context* ctx, const double* G, const double* H, double* Gs,
+                               double* Hs, double* d, int ld, int m)
+{
+  scale_pencil_kernel<<<1, 1024, 0, S(ctx)>>>(G, H, Gs, Hs, d, ld, m);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "scale_pencil");
+}
+
+// C(0:m, 0:k) = D C (undo the scaling of the eigenvector coordinates)
+__global__ void scale_rows_kernel(double* C, const double* d, int ld, int m, int k)
+{
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * k; e += gridDim.x * blockDim.x) {
+    int i = e % m, j = e / m;
+    C[i + (size_t)j * ld] *= d[i];
+  }
+}
+
+extern "C" int gb_scale_rows(gpu_Context* ctx, double* C, const double* d, int ld, int m, int k)
+{
+  scale_rows_kernel<<<small_blocks(m * k), 256, 0, S(ctx)>>>(C, d, ld, m, k);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "scale_rows");
+}
+
+__global__ void small_copy_kernel(const double* A, int lda, double* B, int ldb, int h, int w)
+{
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < h * w; e += gridDim.x * blockDim.x) {
+    int i = e % h, j = e / h;
+    B[i + (size_t)j * ldb] = A[i + (size_t)j * lda];
+  }
+}
+
+extern "C" int gb_small_copy(gpu_Context* ctx, const double* A, int lda, double* B, int ldb, int h,
+                             int w)
+{
+  if (h <= 0 || w <= 0) return 0;
+  small_copy_kernel<<<small_blocks(h * w), 256, 0, S(ctx)>>>(A, lda, B, ldb, h, w);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "small_copy");
 }

@@ -24,7 +24,8 @@ typedef struct {
 /* kernel classes for the event timers */
 enum {
   GB_K_GRAM = 0, GB_K_XC, GB_K_CSR, GB_K_ST7, GB_K_ST5, GB_K_ST27, GB_K_DIAG, GB_K_RESID,
-  GB_K_BLAS1, GB_K_CHOLQR, GB_K_SYGV, GB_K_SMALL, GB_K_TC_GRAM, GB_K_TC_XC, GB_K_COUNT
+  GB_K_BLAS1, GB_K_CHOLQR, GB_K_SYGV, GB_K_SMALL, GB_K_TC_GRAM, GB_K_TC_XC, GB_K_SYGV_FALLBACK,
+  GB_K_RR_CHOL, GB_K_RR_TRSM, GB_K_RR_JAC32, GB_K_RR_GEMM, GB_K_RR_REFINE, GB_K_COUNT
 };
 
 typedef struct {
@@ -58,6 +59,9 @@ struct gpu_Context {
   void** prof_pool; /* free cudaEvent_t */
   int prof_npool;
   lobpcg_gpu_kernel_time prof[GB_K_COUNT];
+  /* device counters: [0] FP32 Jacobi sweeps, [1] largest refinement
+     cluster, [2] FP64 fallback solves, [3] Rayleigh-Ritz calls */
+  int* dcount;
 };
 
 /* error helpers (context.cu) */
@@ -113,6 +117,14 @@ int gb_residual(gpu_Context* ctx, int dtype, long n, const blk_cols* BX, const b
 int gb_drand48_fill(gpu_Context* ctx, int dtype, void* data, long n, long ld, const int* idx,
                     int w, unsigned int seed);
 
+/* tensor-core Gram of the explicit iteration (tc_gram.cu): FP32 blocks X (k
+   columns), R (nR), P (nP) and their images AX, AR, AP; k <= 64, nR, nP <=
+   32 (k <= 32) or 64.  G = [X R P]'[AX AR AP], H = [X R P]'[X R P] (m x m,
+   m = k + nR + nP, FP64, leading dimension ld).  compensated: 3xTF32. */
+int gb_tc_gram(gpu_Context* ctx, long n, const blk_cols* X, int k, const blk_cols* R, int nR,
+               const blk_cols* P, int nP, const blk_cols* AX, const blk_cols* AR,
+               const blk_cols* AP, int compensated, double* G, double* H, int ld);
+
 /* ---------------- small dense FP64 (dense.cu) ---------------- */
 /* in place: A(0:m,0:m) upper Cholesky factor U (A = U'U from the upper
    triangle), then A <- inv(U) with the strict lower part cleared; *info
@@ -126,9 +138,17 @@ int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w, in
 int gb_small_symmetrize(gpu_Context* ctx, double* A, int ld, int m);
 int gb_small_identity(gpu_Context* ctx, double* A, int ld, int h, int w);
 int gb_small_diag(gpu_Context* ctx, double* A, int ld, int m, const double* d);
+/* B(0:h,0:w) = A(0:h,0:w) */
+int gb_small_copy(gpu_Context* ctx, const double* A, int lda, double* B, int ldb, int h, int w);
 /* C(0:h,0:w) = op(A) op(B), inner dimension l (constraints path) */
 int gb_small_gemm(gpu_Context* ctx, const double* A, int lda, int ta, const double* B, int ldb,
                   int tb, double* C, int ldc, int h, int w, int l);
+
+/* explicit-Gram Rayleigh-Ritz helpers: d = 1/sqrt(diag H), Gs = D sym(G) D,
+   Hs = D sym(H) D (unit diagonal); then C(0:m,0:k) <- D C */
+int gb_scale_pencil(gpu_Context* ctx, const double* G, const double* H, double* Gs, double* Hs,
+                    double* d, int ld, int m);
+int gb_scale_rows(gpu_Context* ctx, double* C, const double* d, int ld, int m, int k);
 
 /* ---------------- operators (operators.cu) ---------------- */
 struct gpu_Operator;

@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -386,7 +387,9 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
         ctl->handed_over = 1;
         break;
       }
-      if (mx < 0.9 * best) {
+      /* stagnation at the FP32 floor: no new minimum (by 0.1 %) of the
+         largest active residual for stall_limit iterations */
+      if (mx < 0.999 * best) {
         best = mx;
         stall = 0;
       } else if (++stall >= ctl->stall_limit) {
@@ -561,6 +564,312 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
   return exitflag;
 }
 
+/* ------------------------------------------------- explicit-Gram phase */
+
+static size_t dt_size(int dtype) { return dtype == GPU_MV_FLOAT64 ? 8 : 4; }
+
+/* column table entries for columns idx[0..n) of x, appended at offset */
+static int cols_idx(const gpu_MultiVector* x, const int* idx, int n, blk_cols* t, int off)
+{
+  const char* base = (const char*)x->data;
+  const size_t stride = dt_size(x->dtype) * (size_t)x->ld;
+  for (int c = 0; c < n; c++) t->col[off + c] = base + stride * (idx ? idx[c] : c);
+  return off + n;
+}
+
+static void set_prefix(gpu_MultiVector* x, int n)
+{
+  x->num_active = n;
+  for (int c = 0; c < n; c++) x->active[c] = c;
+}
+
+typedef struct {
+  gpu_MultiVector *Xn, *AXn, *BXn, *Pn, *APn, *BPn;
+  double *G, *H, *Gs, *Hs, *T, *G2, *H2, *tmp, *d, *w;
+  int* infos; /* device: 3 Cholesky status words */
+} explicit_bufs;
+
+/* Block-orthonormalise the explicit pencil on the small side: with U_b the
+   upper Cholesky factor of the b-th diagonal block of H (b = X, R, P),
+   T = blockdiag(inv(U_X), inv(U_R), inv(U_P)), G2 = T'GT, H2 = T'HT.  This is
+   the reference's Cholesky-QR of R and P (lobpcg.c:197-232, 1027-1077)
+   applied to the Gram matrices instead of the n x k blocks.  *bad: bit 1 if
+   R's block is not definite, bit 2 for P's. */
+static int explicit_orthonormalise(solver_t* s, explicit_bufs* eb, int nR, int nP, int* bad)
+{
+  const int k = s->k, k3 = s->k3, m = k + nR + nP;
+  const int off[3] = {0, k, k + nR}, sz[3] = {k, nR, nP};
+  if (gb_small_identity(s->ctx, eb->T, k3, m, m)) return -1;
+  for (int b = 0; b < 3; b++) {
+    if (sz[b] == 0) continue;
+    double* Tb = eb->T + off[b] + (size_t)off[b] * k3;
+    /* T_bb <- H_bb, then inv(chol(H_bb)) in place */
+    if (gb_small_copy(s->ctx, eb->H + off[b] + (size_t)off[b] * k3, k3, Tb, k3, sz[b], sz[b]))
+      return -1;
+    if (gb_cholqr_factor(s->ctx, Tb, k3, sz[b], eb->infos + b)) return -1;
+  }
+  int* hinfo = (int*)gb_pinned(s->ctx, sizeof(int) * 3);
+  if (!hinfo || gb_memcpy_d2h(s->ctx, hinfo, eb->infos, sizeof(int) * 3)) return -1;
+  *bad = (sz[0] && hinfo[0] ? 1 : 0) | (sz[1] && hinfo[1] ? 2 : 0) | (sz[2] && hinfo[2] ? 4 : 0);
+  if (*bad) return 0;
+  /* G2 = T' G T, H2 = T' H T */
+  if (gb_small_gemm(s->ctx, eb->G, k3, 0, eb->T, k3, 0, eb->tmp, k3, m, m, m)) return -1;
+  if (gb_small_gemm(s->ctx, eb->T, k3, 1, eb->tmp, k3, 0, eb->G2, k3, m, m, m)) return -1;
+  if (gb_small_gemm(s->ctx, eb->H, k3, 0, eb->T, k3, 0, eb->tmp, k3, m, m, m)) return -1;
+  if (gb_small_gemm(s->ctx, eb->T, k3, 1, eb->tmp, k3, 0, eb->H2, k3, m, m, m)) return -1;
+  return 0;
+}
+
+/* R(0:nR) = BX(act) diag(lambda(act)) - AX(act), norms of those columns */
+static int explicit_residual(solver_t* s, gpu_MultiVector* X, gpu_MultiVector* AX,
+                             gpu_MultiVector* BX, const int* act, int nR)
+{
+  blk_cols bx, ax, r;
+  cols_idx(BX, act, nR, &bx, 0);
+  cols_idx(AX, act, nR, &ax, 0);
+  cols_idx(s->R, NULL, nR, &r, 0);
+  (void)X;
+  if (gb_residual(s->ctx, s->dt, s->n, &bx, &ax, s->lam, act, &r, nR, s->norm2)) return -1;
+  double* tmp = (double*)gb_pinned(s->ctx, sizeof(double) * s->k);
+  if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->norm2, sizeof(double) * s->k)) return -1;
+  for (int c = 0; c < nR; c++) s->h_norm[act[c]] = sqrt(fabs(tmp[act[c]]));
+  return 0;
+}
+
+/*
+ * The FP32 phase of the mixed mode: block LOBPCG with explicit Gram
+ * matrices.  Each iteration forms G = [X R P]'[AX AR AP] and
+ * H = [X R P]'[BX BR BP] in one pass each (no separate orthonormalisation
+ * passes over R and P), solves the scaled FP64 pencil
+ * (D G D) c = theta (D H D) c on the device -- dropping P when the pencil is
+ * not definite (the restart of lobpcg.c:1056-1063 done on the small side) --
+ * and updates P = [R P] C_RP, X = X C_X + P (and their A / B images) with
+ * one combined kernel each.  Returns 0 (converged, maxit, or handed over to
+ * FP64 with ctl->handed_over set) or -2 on a CUDA error.
+ */
+static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
+{
+  const int k = s->k, k3 = s->k3;
+  int* it = ctl->iteration;
+  int act[BLK_MAXCOLS], prev_act[BLK_MAXCOLS];
+  int nR = k, prev_nR = k, nP = 0, haveP = 0;
+  double best = HUGE_VAL;
+  int stall = 0;
+  gpu_MultiVector *X = s->X, *AX = s->AX, *BX = s->noB ? X : s->BX;
+  gpu_MultiVector *P = s->P, *AP = s->AP, *BP = s->noB ? P : s->BP;
+  gpu_MultiVector *Xn = eb->Xn, *AXn = eb->AXn, *BXn = s->noB ? eb->Xn : eb->BXn;
+  gpu_MultiVector *Pn = eb->Pn, *APn = eb->APn, *BPn = s->noB ? eb->Pn : eb->BPn;
+  gpu_MultiVector *R = s->R, *AR = s->AR, *BR = s->noB ? s->R : s->BR;
+  int rc = 0;
+  /* Gram products on the tensor cores (tcgen05, TF32 products; hi+lo
+     compensated once the residuals are small or TF32 stalls) when the block
+     fits the kernel; else the FP32 CUDA-core kernel */
+  int tc_ok = s->ctx->opt.tensor_cores && s->noB && s->dt == GPU_MV_FLOAT32 && k <= 64;
+  {
+    /* the tensor-core kernel copies 16-byte pieces of every column */
+    const gpu_MultiVector* blocks[8] = {X, AX, P, AP, Xn, AXn, Pn, APn};
+    for (int b = 0; b < 8; b++)
+      if (((uintptr_t)blocks[b]->data & 15) || (blocks[b]->ld & 3)) tc_ok = 0;
+    if (((uintptr_t)R->data & 15) || (R->ld & 3) || ((uintptr_t)AR->data & 15) || (AR->ld & 3) ||
+        ((uintptr_t)s->W->data & 15) || (s->W->ld & 3))
+      tc_ok = 0;
+  }
+  int comp = 0;
+  for (int i = 0; i < k; i++) prev_act[i] = i;  /* phase_setup left R for all columns */
+  gb_mv_set_mask_host(X, NULL);
+  gb_mv_set_mask_host(AX, NULL);
+
+  for (*it = ctl->it_base + 1; *it <= ctl->maxit; (*it)++) {
+    nR = 0;
+    for (int i = 0; i < k; i++) {
+      s->mask[i] = s->h_norm[i] > fabs(s->h_lam[i]) * s->tol.relative + s->tol.absolute + DBL_EPSILON;
+      if (s->mask[i]) act[nR++] = i;
+    }
+    if (nR < 1) break;
+    nP = haveP ? nR : 0; /* P restricted to the active columns */
+    {
+      double mx = 0.0;
+      for (int c = 0; c < nR; c++)
+        if (s->h_norm[act[c]] > mx) mx = s->h_norm[act[c]];
+      if (mx < ctl->fp64_below) {
+        ctl->handed_over = 1;
+        break;
+      }
+      if (tc_ok && !comp && mx < s->ctx->opt.compensated_below) {
+        comp = 1;
+        stall = 0;
+      }
+      if (mx < 0.999 * best) {
+        best = mx;
+        stall = 0;
+      } else if (++stall >= ctl->stall_limit) {
+        if (tc_ok && !comp) {
+          comp = 1; /* TF32 products stalled: compensate before FP64 */
+          stall = 0;
+        } else {
+          ctl->handed_over = 1;
+          break;
+        }
+      }
+    }
+    /* the residual block must hold exactly the active columns */
+    if (nR != prev_nR || memcmp(act, prev_act, sizeof(int) * nR)) {
+      if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
+    }
+    set_prefix(R, nR);
+    set_prefix(AR, nR);
+    set_prefix(s->W, nR);
+    if (!s->noB) set_prefix(BR, nR);
+    if (!s->noT) {
+      gpu_MultiVector* t;
+      if (d_apply(s, s->T, s->Tdata, R, s->W)) return -2;
+      t = R;
+      R = s->W;
+      s->W = t;
+      if (s->noB) BR = R;
+      s->R = R;
+    }
+    if (!s->noY && project_constraints(s, R)) return -2;
+    if (!s->noB && d_apply(s, s->B, s->Bdata, R, BR)) return -2;
+    if (d_apply(s, s->A, s->Adata, R, AR)) return -2;
+
+    /* Gram matrices of [X R P(act)] */
+    {
+      blk_cols left, right;
+      int m, off;
+      off = cols_idx(X, NULL, k, &left, 0);
+      off = cols_idx(R, NULL, nR, &left, off);
+      m = cols_idx(P, act, nP, &left, off);
+      off = cols_idx(AX, NULL, k, &right, 0);
+      off = cols_idx(AR, NULL, nR, &right, off);
+      cols_idx(AP, act, nP, &right, off);
+      if (tc_ok) {
+        blk_cols cx, cr, cp, cax, car, cap;
+        cols_idx(X, NULL, k, &cx, 0);
+        cols_idx(R, NULL, nR, &cr, 0);
+        cols_idx(P, act, nP, &cp, 0);
+        cols_idx(AX, NULL, k, &cax, 0);
+        cols_idx(AR, NULL, nR, &car, 0);
+        cols_idx(AP, act, nP, &cap, 0);
+        if (gb_tc_gram(s->ctx, s->n, &cx, k, &cr, nR, &cp, nP, &cax, &car, &cap, comp, eb->G,
+                       eb->H, k3))
+          return -2;
+        if (comp) s->ctx->stats.iterations_compensated++;
+      } else {
+        if (gb_gram(s->ctx, s->dt, s->n, &left, m, &right, m, eb->G, k3)) return -2;
+        off = cols_idx(BX, NULL, k, &right, 0);
+        off = cols_idx(BR, NULL, nR, &right, off);
+        cols_idx(BP, act, nP, &right, off);
+        if (gb_gram(s->ctx, s->dt, s->n, &left, m, &right, m, eb->H, k3)) return -2;
+      }
+
+      /* Rayleigh-Ritz on the block-orthonormalised pencil; without P when
+         P's block or the pencil is not definite (lobpcg.c:1056-1063) */
+      int info = 1, bad = 0;
+      int use_p = nP;
+      if (explicit_orthonormalise(s, eb, nR, nP, &bad)) return -2;
+      if (bad & 3) {
+        ctl->handed_over = 1; /* X or R cannot be orthonormalised in FP32 */
+        break;
+      }
+      if (bad & 4) {
+        use_p = 0;
+        if (explicit_orthonormalise(s, eb, nR, 0, &bad)) return -2;
+        if (bad) {
+          ctl->handed_over = 1;
+          break;
+        }
+      }
+      while (1) {
+        int mm = k + nR + use_p;
+        if (gb_small_copy(s->ctx, eb->G2, k3, eb->Gs, k3, mm, mm) ||
+            gb_small_copy(s->ctx, eb->H2, k3, eb->Hs, k3, mm, mm))
+          return -2;
+        if (gb_sygv(s->ctx, eb->Gs, eb->Hs, k3, mm, eb->w, s->info) || read_info(s, &info))
+          return -2;
+        if (info == 0 || use_p == 0) break;
+        use_p = 0;
+        if (explicit_orthonormalise(s, eb, nR, 0, &bad)) return -2;
+        if (bad) break;
+      }
+      if (info != 0 || bad) {
+        ctl->handed_over = 1;
+        break;
+      }
+      const int mm = k + nR + use_p;
+      /* coordinates in the original basis: C = T C' (first k columns) */
+      if (gb_small_gemm(s->ctx, eb->T, k3, 0, eb->Gs, k3, 0, eb->tmp, k3, mm, k, mm)) return -2;
+      if (gb_small_copy(s->ctx, eb->tmp, k3, eb->Gs, k3, mm, k)) return -2;
+      if (gb_memcpy_d2d(s->ctx, s->lam, eb->w, sizeof(double) * k)) return -2;
+
+      /* P = [R P(act)] C_RP ; X = X C_X + P, and the A / B images */
+      const double* cX = eb->Gs;
+      const double* cRP = eb->Gs + k;
+      const int h = nR + use_p;
+      gpu_MultiVector* srcs[3][3] = {{R, P, Pn}, {AR, AP, APn}, {BR, BP, BPn}};
+      gpu_MultiVector* xs[3][2] = {{X, Xn}, {AX, AXn}, {BX, BXn}};
+      const int nsets = s->noB ? 2 : 3;
+      for (int q = 0; q < nsets; q++) {
+        blk_cols a, y, z, xa;
+        int off2 = cols_idx(srcs[q][0], NULL, nR, &a, 0);
+        cols_idx(srcs[q][1], act, use_p, &a, off2);
+        cols_idx(srcs[q][2], NULL, k, &y, 0);
+        if (gb_bymat(s->ctx, s->dt, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
+        cols_idx(xs[q][0], NULL, k, &xa, 0);
+        cols_idx(xs[q][1], NULL, k, &z, 0);
+        if (gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
+      }
+      /* swap the double buffers */
+      gpu_MultiVector* t;
+      t = X; X = Xn; Xn = t;
+      t = AX; AX = AXn; AXn = t;
+      t = P; P = Pn; Pn = t;
+      t = AP; AP = APn; APn = t;
+      if (!s->noB) {
+        t = BX; BX = BXn; BXn = t;
+        t = BP; BP = BPn; BPn = t;
+      } else {
+        BX = X;
+        BXn = Xn;
+        BP = P;
+        BPn = Pn;
+      }
+      haveP = 1; /* P holds all k columns from now on */
+    }
+
+    /* residuals of the active columns and the new Ritz values */
+    if (fetch_lambda(s)) return -2;
+    if (nonfinite(s->h_lam, k)) {
+      ctl->handed_over = 1;
+      break;
+    }
+    if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
+    prev_nR = nR;
+    memcpy(prev_act, act, sizeof(int) * nR);
+    {
+      const int col = *it;
+      if (ctl->lam_hist && col <= ctl->maxit)
+        memcpy(ctl->lam_hist + (size_t)col * ctl->lam_gh, s->h_lam, sizeof(double) * k);
+      if (ctl->res_hist && col <= ctl->maxit)
+        memcpy(ctl->res_hist + (size_t)col * ctl->res_gh, s->h_norm, sizeof(double) * k);
+    }
+    if (s->verbosity == 2) {
+      printf("Iteration %d \tbsize %d\n", *it, nR);
+      dump_lambda(s->h_norm, s->h_lam, *it, k);
+    } else if (s->verbosity == 1) {
+      printf("Iteration %d \tbsize %d \tmaxres %22.14e\n", *it, nR, max_value(s->h_norm, k));
+    }
+  }
+  /* the phase's block lives in s->X for the hand-over */
+  if (X != s->X) {
+    gb_mv_set_mask_host(X, NULL);
+    gb_mv_set_mask_host(s->X, NULL);
+    rc = d_copy(s, X, s->X);
+  }
+  s->R = R;
+  return rc ? -2 : 0;
+}
+
 /* ------------------------------------------------------------ the API */
 
 static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_fn B, void* Tdata,
@@ -576,6 +885,7 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
 
   memset(&s, 0, sizeof(s));
   memset(&ctx->stats, 0, sizeof(ctx->stats));
+  cudaMemsetAsync(ctx->dcount, 0, 8 * sizeof(int), (cudaStream_t)ctx->stream);
   ctx->err[0] = 0;
   ctx->potrf_calls = 0;
   ctx->sygv_calls = 0;
@@ -701,6 +1011,37 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
         }
       }
       exitflag = phase_setup(&s);
+      explicit_bufs eb;
+      int have_eb = 0;
+      memset(&eb, 0, sizeof(eb));
+      if (exitflag == 0 && phase == 0) {
+        /* buffers of the explicit-Gram FP32 phase */
+        const size_t sq = (size_t)s.k3 * s.k3;
+        eb.Xn = gb_mv_create_like(s.X, s.dt);
+        eb.AXn = gb_mv_create_like(s.X, s.dt);
+        eb.Pn = gb_mv_create_like(s.X, s.dt);
+        eb.APn = gb_mv_create_like(s.X, s.dt);
+        if (!s.noB) {
+          eb.BXn = gb_mv_create_like(s.X, s.dt);
+          eb.BPn = gb_mv_create_like(s.X, s.dt);
+        }
+        eb.G = (double*)gb_device_alloc(ctx, sizeof(double) * (8 * sq + 2 * (size_t)s.k3) + 64);
+        have_eb = 1;
+        if (!eb.Xn || !eb.AXn || !eb.Pn || !eb.APn || !eb.G || (!s.noB && (!eb.BXn || !eb.BPn))) {
+          exitflag = -2;
+        } else {
+          eb.H = eb.G + sq;
+          eb.Gs = eb.H + sq;
+          eb.Hs = eb.Gs + sq;
+          eb.T = eb.Hs + sq;
+          eb.G2 = eb.T + sq;
+          eb.H2 = eb.G2 + sq;
+          eb.tmp = eb.H2 + sq;
+          eb.d = eb.tmp + sq;
+          eb.w = eb.d + s.k3;
+          eb.infos = (int*)(eb.w + s.k3);
+        }
+      }
       if (exitflag == 0 && (phase == 1 || !mixed)) {
         /* the setup of the (last) FP64 phase: record it as iteration 0 when
            no FP32 iterations ran */
@@ -724,9 +1065,12 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
         ctl.it_base = *iterationNumber;
         ctl.stop_fp32 = phase == 0;
         ctl.fp64_below = ctx->opt.fp64_below;
-        ctl.stall_limit = ctx->opt.fp32_stall > 0 ? ctx->opt.fp32_stall : 10;
+        ctl.stall_limit = ctx->opt.fp32_stall > 0 ? ctx->opt.fp32_stall : 20;
         ctl.handed_over = 0;
-        exitflag = phase_loop(&s, &ctl);
+        if (phase == 0)
+          exitflag = phase_explicit(&s, &ctl, &eb);
+        else
+          exitflag = phase_loop(&s, &ctl);
         if (phase == 0) {
           /* the loop counter points one past the last finished iteration */
           int done_its = *iterationNumber - 1;
@@ -741,6 +1085,16 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           ctx->stats.iterations_fp64 = *iterationNumber - 1 - ctl.it_base;
           ctx->stats.seconds_fp64 = gb_now() - tp;
         }
+      }
+      if (have_eb) {
+        gpu_MultiVectorDestroy(eb.Xn);
+        gpu_MultiVectorDestroy(eb.AXn);
+        gpu_MultiVectorDestroy(eb.Pn);
+        gpu_MultiVectorDestroy(eb.APn);
+        gpu_MultiVectorDestroy(eb.BXn);
+        gpu_MultiVectorDestroy(eb.BPn);
+        gb_sync(ctx);
+        gb_device_free(eb.G);
       }
       if (!s.noY) {
         if (!s.noB && s.BY != s.Y) gpu_MultiVectorDestroy(s.BY);
@@ -787,6 +1141,15 @@ done:
     for (int i = 0; i < s.k; i++)
       if (resNorms[i] > mx) mx = resNorms[i];
     ctx->stats.final_max_residual = mx;
+  }
+  {
+    int* c = (int*)gb_pinned(ctx, 8 * sizeof(int));
+    if (c && gb_memcpy_d2h(ctx, c, ctx->dcount, 8 * sizeof(int)) == 0) {
+      ctx->stats.rr_jacobi32_sweeps = c[0];
+      ctx->stats.rr_max_cluster = c[1];
+      ctx->stats.rr_fallbacks = c[2];
+      ctx->stats.rr_calls = c[3];
+    }
   }
   ctx->stats.seconds_total = gb_now() - t0;
   ctx->stats.kernel_launches = gpu_KernelLaunchCount() - launches0;

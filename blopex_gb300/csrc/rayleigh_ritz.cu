@@ -3,26 +3,28 @@
 // lobpcg_solveGEVP (blopex_abstract/krylov/lobpcg.c:66-103), built for a GPU
 // whose FP32 rate is 64 times its FP64 rate:
 //
-//   1. FP32, one CTA: Cholesky B = L L', C = inv(L) A inv(L)'          (rr_reduce32)
-//   2. FP32, cyclic Jacobi on C; every CTA rotates its own copy of C
+//   1. FP64, one CTA: Cholesky B = L L' (its failure is dsygv's INFO m+j)
+//   2. FP64, multi-CTA triangular solves: C = inv(L) A inv(L)'   -- the
+//      conditioning of B is handled here, in FP64, as dsygv does
+//   3. FP32, cyclic Jacobi on C; every CTA rotates its own copy of C
 //      (identical arithmetic, no communication) and accumulates its own
-//      slice of rows of the eigenvector matrix V                       (rr_jacobi32)
-//   3. FP32, X = inv(L)' V sorted by eigenvalue, widened to FP64         (rr_backsub32)
-//   4. FP64 refinement of the eigenvector matrix, twice: with
-//      S = X'AX and P = X'BX (multi-CTA FP64 GEMMs), the Ritz values
-//      l_i = S_ii / P_ii and the correction X <- X (I + E),
+//      slice of rows of the eigenvector matrix V
+//   4. FP64 refinement of V, twice: with S = V'CV and P = V'V
+//      (multi-CTA FP64 GEMMs), the Ritz values l_i = S_ii / P_ii and the
+//      correction V <- V (I + E),
 //        E_ij = (S_ij - l_j P_ij) / (l_j - l_i)   for separated pairs,
 //        E_ij = R_ij / 2 with R = I - P           inside clusters,
 //      and inside each cluster of close values the FP64 matrix
 //      S_cc + (R_cc S_cc + S_cc R_cc)/2 is diagonalised by FP64 Jacobi.
 //      This is the iterative refinement of Ogita & Aishima (symmetric
-//      eigenproblems, Japan J. Indust. Appl. Math. 2018) written for the
-//      B-inner product; each round squares the eigenvector error.
-//   5. the first m columns of X and the values go to A and w (dsygv's
-//      outputs; B is left intact).
-// If the FP32 Cholesky or Jacobi fails, the one-CTA FP64 Jacobi solver of
-// dense.cu runs instead (gated on a device status word, no host sync).
-// Every loop has a fixed trip count.
+//      eigenproblems, Japan J. Indust. Appl. Math. 2018); each round
+//      squares the eigenvector error.
+//   5. FP64, multi-CTA: eigenvectors of the pencil inv(L)' V into A, values
+//      into w (dsygv's outputs; B is left intact).
+// If the FP32 Jacobi does not converge or the refinement does not settle,
+// the one-CTA FP64 Jacobi solver of dense.cu runs on the original pencil
+// instead (gated on a device status word, no host sync).  Every loop has a
+// fixed trip count.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -38,18 +40,21 @@ static inline cudaStream_t S_(gpu_Context* ctx) { return (cudaStream_t)ctx->stre
 
 // status words (device ints): [0] fast path failed, [1] Jacobi32 sweeps
 struct rr_scratch {
-  float *L, *C, *W, *V, *lam32;
-  double *X, *Xn, *TA, *TB, *S, *P, *EI, *Q, *F, *J1, *J2, *lam;
+  int* count;  // context counters (see internal.h)
+  float *C, *V, *lam32;
+  double *L64, *LT64, *C64, *W64;
+  double *X, *Xn, *TA, *S, *P, *EI, *Q, *F, *J1, *J2, *lam;
   int* status;
 };
 
 // ------------------------------------------------------------------ 1.
-__global__ void __launch_bounds__(RR_THREADS) rr_reduce32_kernel(const double* __restrict__ A,
-                                                                 const double* __restrict__ B,
-                                                                 int ld, int m, rr_scratch s)
+// FP64 lower Cholesky of B into s.L64 (m x m, ld m); *info = m + j on
+// failure (dsygv's convention for a B that is not positive definite).
+__global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __restrict__ B, int ld,
+                                                               int m, rr_scratch s, int* info)
 {
-  extern __shared__ float Ls[];  // m*m, column-major
   __shared__ int bad;
+  double* L = s.L64;
   const int tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) {
     bad = 0;
@@ -57,61 +62,125 @@ __global__ void __launch_bounds__(RR_THREADS) rr_reduce32_kernel(const double* _
   }
   for (int e = tid; e < m * m; e += nt) {
     int i = e % m, j = e / m;
-    Ls[e] = (i >= j) ? (float)B[i + (size_t)j * ld] : 0.f;
+    L[e] = (i >= j) ? B[i + (size_t)j * ld] : 0.0;
   }
   __syncthreads();
-  // right-looking Cholesky, lower
   for (int j = 0; j < m; j++) {
     if (tid == 0) {
-      float d = Ls[j + j * m];
-      if (!(d > 0.f) || !isfinite(d))
-        bad = 1;
+      double d = L[j + (size_t)j * m];
+      if (!(d > 0.0) || !isfinite(d))
+        bad = j + 1;
       else
-        Ls[j + j * m] = sqrtf(d);
+        L[j + (size_t)j * m] = sqrt(d);
     }
     __syncthreads();
     if (bad) break;
-    const float djj = Ls[j + j * m];
-    for (int i = j + 1 + tid; i < m; i += nt) Ls[i + j * m] /= djj;
+    const double djj = L[j + (size_t)j * m];
+    for (int i = j + 1 + tid; i < m; i += nt) L[i + (size_t)j * m] /= djj;
     __syncthreads();
     const int r = m - j - 1;
     for (int e = tid; e < r * r; e += nt) {
       int i = j + 1 + e % r, l = j + 1 + e / r;
-      if (i >= l) Ls[i + l * m] -= Ls[i + j * m] * Ls[l + j * m];
+      if (i >= l) L[i + (size_t)l * m] -= L[i + (size_t)j * m] * L[l + (size_t)j * m];
     }
     __syncthreads();
   }
   if (bad) {
-    if (tid == 0) s.status[0] = 1;
+    if (tid == 0) {
+      s.status[0] = 5;
+      *info = m + bad;
+    }
     return;
   }
-  for (int e = tid; e < m * m; e += nt) s.L[e] = Ls[e];
-  // W = inv(L) A, one thread per column, A symmetric from its lower triangle
-  for (int j = tid; j < m; j += nt) {
-    float* w = s.W + (size_t)j * m;
-    for (int i = 0; i < m; i++) {
-      float a = (float)((i >= j) ? A[i + (size_t)j * ld] : A[j + (size_t)i * ld]);
-      for (int p = 0; p < i; p++) a -= Ls[i + p * m] * w[p];
-      w[i] = a / Ls[i + i * m];
-    }
-  }
-  __syncthreads();
-  // C = inv(L) W' (column j of C solves L c = row j of W)
-  for (int j = tid; j < m; j += nt) {
-    float* c = s.C + (size_t)j * m;
-    for (int i = 0; i < m; i++) {
-      float a = s.W[j + (size_t)i * m];
-      for (int p = 0; p < i; p++) a -= Ls[i + p * m] * c[p];
-      c[i] = a / Ls[i + i * m];
-    }
-  }
-  __syncthreads();
   for (int e = tid; e < m * m; e += nt) {
+    int i = e % m, p = e / m;
+    s.LT64[p + (size_t)i * m] = L[e];
+  }
+}
+
+// triangular solves with the FP64 factor, one warp per right-hand side; the
+// solution lives in registers (entry p in lane p % 32, slot p / 32):
+//   mode 0: X = inv(L) Y, Y symmetric read from its lower triangle (ld ldy)
+//   mode 1: X = inv(L) Y' (Y m x m, ld ldy)
+//   mode 2: X = inv(L)' Y (Y m x m, ld ldy), result to X with leading dim ldx
+// s.LT holds L row-major (LT[p + i*m] = L(i, p)) so that the forward
+// sweeps read contiguous rows of L.
+#define RR_TRSM_SLOTS (RR_MAX_SMEM_M / 32)
+__global__ void __launch_bounds__(256) rr_trsm64_kernel(int mode, const double* __restrict__ Y,
+                                                        int ldy, double* __restrict__ X, int ldx,
+                                                        int m, rr_scratch s)
+{
+  if (s.status[0]) return;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= m) return;
+  double xr[RR_TRSM_SLOTS];
+#pragma unroll
+  for (int q = 0; q < RR_TRSM_SLOTS; q++) xr[q] = 0.0;
+  if (mode < 2) {
+    const double* LT = s.LT64;
+    for (int i = 0; i < m; i++) {
+      double part = 0.0;
+#pragma unroll
+      for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+        int p = q * 32 + lane;
+        if (p < i) part += LT[p + (size_t)i * m] * xr[q];
+      }
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      double a;
+      if (mode == 0)
+        a = (i >= j) ? Y[i + (size_t)j * ldy] : Y[j + (size_t)i * ldy];
+      else
+        a = Y[j + (size_t)i * ldy];
+      const double xi = (a - part) / LT[i + (size_t)i * m];
+#pragma unroll
+      for (int q = 0; q < RR_TRSM_SLOTS; q++)
+        if (q * 32 + lane == i) xr[q] = xi;
+    }
+  } else {
+    const double* L = s.L64;
+    for (int i = m - 1; i >= 0; i--) {
+      double part = 0.0;
+#pragma unroll
+      for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+        int p = q * 32 + lane;
+        if (p > i && p < m) part += L[p + (size_t)i * m] * xr[q];
+      }
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const double xi = (Y[i + (size_t)j * ldy] - part) / L[i + (size_t)i * m];
+#pragma unroll
+      for (int q = 0; q < RR_TRSM_SLOTS; q++)
+        if (q * 32 + lane == i) xr[q] = xi;
+    }
+  }
+  double* x = X + (size_t)j * ldx;
+#pragma unroll
+  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+    int p = q * 32 + lane;
+    if (p < m) x[p] = xr[q];
+  }
+}
+
+// symmetrise the FP64 reduced matrix and make the FP32 copy for Jacobi
+__global__ void rr_sym_kernel(int m, rr_scratch s)
+{
+  if (s.status[0]) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * m; e += gridDim.x * blockDim.x) {
+    int i = e % m, j = e / m;
+    double v = 0.5 * (s.C64[i + (size_t)j * m] + s.C64[j + (size_t)i * m]);
+    s.C[e] = (float)v;
+  }
+}
+
+__global__ void rr_sym_store_kernel(int m, rr_scratch s)
+{
+  if (s.status[0]) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * m; e += gridDim.x * blockDim.x) {
     int i = e % m, j = e / m;
     if (i > j) {
-      float v = 0.5f * (s.C[i + (size_t)j * m] + s.C[j + (size_t)i * m]);
-      s.C[i + (size_t)j * m] = v;
-      s.C[j + (size_t)i * m] = v;
+      double v = 0.5 * (s.C64[i + (size_t)j * m] + s.C64[j + (size_t)i * m]);
+      s.C64[i + (size_t)j * m] = v;
+      s.C64[j + (size_t)i * m] = v;
     }
   }
 }
@@ -127,11 +196,107 @@ __device__ __forceinline__ void rr_pair(int t, int round, int me, int* p, int* q
   *q = max(pa, pb);
 }
 
+
+// One cyclic-Jacobi sweep structure shared by the FP32 and FP64 solvers.
+// A round pairs every index with one partner (tournament ordering); the
+// rotations of a round are disjoint, so C <- J' C J is applied as
+// independent 2x2 blocks (rows of pair t, columns of pair u): one pass and
+// two barriers per round.  Columns of V (rows r0..r0+nr of it) rotate in
+// the same pass.  C is m x m with leading dimension lc; V rows have stride lv.
+template <typename T>
+__device__ int rr_jacobi_rounds(T* C, int m, int lc, T* V, int nr, int lv, T thr_rot,
+                                T thr_done, int max_sweeps, T* s_c, T* s_s, int* s_p, int* s_q,
+                                int* s_done, int* sweeps_out)
+{
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const int me = (m + 1) & ~1, half = me / 2;
+  int converged = 0, sweep = 0;
+  for (; sweep < max_sweeps && !converged; sweep++) {
+    if (tid == 0) *s_done = 1;
+    __syncthreads();
+    for (int round = 0; round < me - 1; round++) {
+      for (int t = tid; t < half; t += nt) {
+        int p, q;
+        rr_pair(t, round, me, &p, &q);
+        T c = T(1), sn = T(0);
+        if (q < m) {
+          T apq = C[p + q * lc], app = C[p + p * lc], aqq = C[q + q * lc];
+          if (fabs((double)apq) > (double)thr_rot) {
+            T theta = (aqq - app) / (T(2) * apq);
+            T tt = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(T(1) + theta * theta));
+            c = T(1) / sqrt(T(1) + tt * tt);
+            sn = tt * c;
+            if (fabs((double)apq) > (double)thr_done) *s_done = 0;
+          }
+        } else {
+          q = p;  // the dummy partner of an odd order
+        }
+        s_p[t] = p;
+        s_q[t] = q;
+        s_c[t] = c;
+        s_s[t] = sn;
+      }
+      __syncthreads();
+      // 2x2 blocks (pair t rows, pair u columns): warp strides t, lane strides u
+      for (int t = warp; t < half; t += nwarp) {
+        const int p = s_p[t], q = s_q[t];
+        const T ct = s_c[t], st = s_s[t];
+        for (int u = lane; u < half; u += 32) {
+          const T su = s_s[u];
+          if (st == T(0) && su == T(0)) continue;
+          const int pu = s_p[u], qu = s_q[u];
+          const T cu = s_c[u];
+          const int twoq = (q != p), twou = (qu != pu);
+          T a = C[p + pu * lc], b = twou ? C[p + qu * lc] : T(0);
+          T c2 = twoq ? C[q + pu * lc] : T(0), d = (twoq && twou) ? C[q + qu * lc] : T(0);
+          // right rotation by pair u (columns pu, qu)
+          T a1 = cu * a - su * b, b1 = su * a + cu * b;
+          T c1 = cu * c2 - su * d, d1 = su * c2 + cu * d;
+          // left rotation by pair t (rows p, q)
+          T a2 = ct * a1 - st * c1, c3 = st * a1 + ct * c1;
+          T b2 = ct * b1 - st * d1, d2 = st * b1 + ct * d1;
+          if (t == u && twoq) {  // the annihilated entry
+            b2 = T(0);
+            c3 = T(0);
+          }
+          C[p + pu * lc] = a2;
+          if (twou) C[p + qu * lc] = b2;
+          if (twoq) C[q + pu * lc] = c3;
+          if (twoq && twou) C[q + qu * lc] = d2;
+        }
+      }
+      // V <- V J for the local rows: warp strides rows, lane strides pairs
+      for (int r = warp; r < nr; r += nwarp) {
+        for (int u = lane; u < half; u += 32) {
+          const T su = s_s[u];
+          if (su == T(0)) continue;
+          const int pu = s_p[u], qu = s_q[u];
+          const T cu = s_c[u];
+          T vp = V[r * lv + pu], vq = V[r * lv + qu];
+          V[r * lv + pu] = cu * vp - su * vq;
+          V[r * lv + qu] = su * vp + cu * vq;
+        }
+      }
+      __syncthreads();
+    }
+    converged = *s_done;
+    __syncthreads();
+  }
+  *sweeps_out = sweep;
+  return converged;
+}
+
+// shared-memory layouts use an odd leading dimension so that both the row
+// and the column sweeps of a rotation hit 32 different banks
+__host__ __device__ __forceinline__ int rr_pad(int m) { return m | 1; }
+
 __global__ void __launch_bounds__(RR_THREADS) rr_jacobi32_kernel(int m, int rows, rr_scratch s)
 {
   extern __shared__ float sm[];
-  float* Cs = sm;            // m*m
-  float* Vs = sm + m * m;    // rows*m: rows r0..r0+rows of V, row-major by V row
+  const int lc = rr_pad(m);
+  float* Cs = sm;             // m x m, column-major, leading dimension lc
+  float* Vs = sm + m * lc;    // rows x m slice of V, row r at Vs + r*lc (V^T layout)
   __shared__ float s_c[256], s_s[256];
   __shared__ int s_p[256], s_q[256];
   __shared__ int s_done;
@@ -140,13 +305,12 @@ __global__ void __launch_bounds__(RR_THREADS) rr_jacobi32_kernel(int m, int rows
   const int r0 = blockIdx.x * rows;
   const int nr = min(rows, m - r0);
   if (s.status[0]) return;
-  for (int e = tid; e < m * m; e += nt) Cs[e] = s.C[e];
-  for (int e = tid; e < rows * m; e += nt) {
-    int r = e / m, c = e % m;
-    Vs[e] = (r0 + r == c) ? 1.f : 0.f;
-  }
+  for (int j = 0; j < m; j++)
+    for (int i = tid; i < m; i += nt) Cs[i + j * lc] = s.C[i + (size_t)j * m];
+  for (int r = 0; r < rows; r++)
+    for (int c = tid; c < m; c += nt) Vs[r * lc + c] = (r0 + r == c) ? 1.f : 0.f;
   float acc = 0.f;
-  for (int e = tid; e < m * m; e += nt) acc += Cs[e] * Cs[e];
+  for (int e = tid; e < m * m; e += nt) acc += s.C[e] * s.C[e];
   s_red[tid] = acc;
   __syncthreads();
   for (int o = nt / 2; o > 0; o >>= 1) {
@@ -154,98 +318,33 @@ __global__ void __launch_bounds__(RR_THREADS) rr_jacobi32_kernel(int m, int rows
     __syncthreads();
   }
   const float nrm = sqrtf(s_red[0]);
-  const float thr_rot = 0.05f * FLT_EPSILON * nrm;
-  const float thr_done = 8.f * FLT_EPSILON * nrm;
-  const int me = (m + 1) & ~1, half = me / 2;
-  int converged = 0, sweep = 0;
-  for (; sweep < JACOBI32_MAX_SWEEPS && !converged; sweep++) {
-    if (tid == 0) s_done = 1;
-    __syncthreads();
-    for (int round = 0; round < me - 1; round++) {
-      for (int t = tid; t < half; t += nt) {
-        int p, q;
-        rr_pair(t, round, me, &p, &q);
-        float c = 1.f, sn = 0.f;
-        if (q < m) {
-          float apq = Cs[p + q * m], app = Cs[p + p * m], aqq = Cs[q + q * m];
-          if (fabsf(apq) > thr_rot) {
-            float theta = (aqq - app) / (2.f * apq);
-            float tt = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(1.f + theta * theta));
-            c = rsqrtf(1.f + tt * tt);
-            sn = tt * c;
-            if (fabsf(apq) > thr_done) s_done = 0;
-          }
-        }
-        s_p[t] = p;
-        s_q[t] = q;
-        s_c[t] = c;
-        s_s[t] = sn;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {
-        int t = e / m, j = e % m;
-        float sn = s_s[t];
-        if (sn == 0.f) continue;
-        int p = s_p[t], q = s_q[t];
-        float c = s_c[t];
-        float ap = Cs[p + j * m], aq = Cs[q + j * m];
-        Cs[p + j * m] = c * ap - sn * aq;
-        Cs[q + j * m] = sn * ap + c * aq;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {
-        int t = e / m, i = e % m;
-        float sn = s_s[t];
-        if (sn == 0.f) continue;
-        int p = s_p[t], q = s_q[t];
-        float c = s_c[t];
-        float ap = Cs[i + p * m], aq = Cs[i + q * m];
-        Cs[i + p * m] = c * ap - sn * aq;
-        Cs[i + q * m] = sn * ap + c * aq;
-      }
-      for (int e = tid; e < half * nr; e += nt) {
-        int t = e / nr, r = e % nr;
-        float sn = s_s[t];
-        if (sn == 0.f) continue;
-        int p = s_p[t], q = s_q[t];
-        float c = s_c[t];
-        float vp = Vs[r * m + p], vq = Vs[r * m + q];
-        Vs[r * m + p] = c * vp - sn * vq;
-        Vs[r * m + q] = sn * vp + c * vq;
-      }
-      __syncthreads();
-      for (int t = tid; t < half; t += nt)
-        if (s_s[t] != 0.f) {
-          Cs[s_p[t] + s_q[t] * m] = 0.f;
-          Cs[s_q[t] + s_p[t] * m] = 0.f;
-        }
-      __syncthreads();
-    }
-    converged = s_done;
-    __syncthreads();
-  }
+  int sweeps = 0;
+  int converged = rr_jacobi_rounds<float>(Cs, m, lc, Vs, nr, lc, 0.05f * FLT_EPSILON * nrm,
+                                          8.f * FLT_EPSILON * nrm, JACOBI32_MAX_SWEEPS, s_c, s_s,
+                                          s_p, s_q, &s_done, &sweeps);
   if (!converged) {
     if (tid == 0) s.status[0] = 2;
     return;
   }
-  for (int e = tid; e < nr * m; e += nt) {
-    int r = e / m, c = e % m;
-    s.V[(r0 + r) + (size_t)c * m] = Vs[r * m + c];
-  }
+  for (int r = 0; r < nr; r++)
+    for (int c = tid; c < m; c += nt) s.V[(r0 + r) + (size_t)c * m] = Vs[r * lc + c];
   if (blockIdx.x == 0) {
-    for (int i = tid; i < m; i += nt) s.lam32[i] = Cs[i + i * m];
-    if (tid == 0) s.status[1] = sweep;
+    for (int i = tid; i < m; i += nt) s.lam32[i] = Cs[i + i * lc];
+    if (tid == 0) {
+      s.status[1] = sweeps;
+      atomicAdd(&s.count[0], sweeps);
+      atomicAdd(&s.count[3], 1);
+    }
   }
 }
 
 // ------------------------------------------------------------------ 3.
-__global__ void __launch_bounds__(RR_THREADS) rr_backsub32_kernel(int m, rr_scratch s)
+// eigenvectors of C sorted by the FP32 eigenvalues, widened to FP64
+__global__ void __launch_bounds__(RR_THREADS) rr_vsort_kernel(int m, rr_scratch s)
 {
-  extern __shared__ float Ls[];
   __shared__ int perm[512];
   const int tid = threadIdx.x, nt = blockDim.x;
   if (s.status[0]) return;
-  for (int e = tid; e < m * m; e += nt) Ls[e] = s.L[e];
   for (int i = tid; i < m; i += nt) {
     float di = s.lam32[i];
     int r = 0;
@@ -256,17 +355,9 @@ __global__ void __launch_bounds__(RR_THREADS) rr_backsub32_kernel(int m, rr_scra
     perm[r] = i;
   }
   __syncthreads();
-  // x = inv(L)' v, one thread per output column; accumulate in FP32 then widen
-  for (int r = tid; r < m; r += nt) {
-    const float* v = s.V + (size_t)perm[r] * m;
-    double* x = s.X + (size_t)r * m;
-    float* tmp = s.W + (size_t)r * m;  // W is free scratch now
-    for (int i = m - 1; i >= 0; i--) {
-      float a = v[i];
-      for (int p = i + 1; p < m; p++) a -= Ls[p + i * m] * tmp[p];
-      tmp[i] = a / Ls[i + i * m];
-      x[i] = (double)tmp[i];
-    }
+  for (int e = tid; e < m * m; e += nt) {
+    int i = e % m, r = e / m;
+    s.X[i + (size_t)r * m] = (double)s.V[i + (size_t)perm[r] * m];
   }
 }
 
@@ -329,18 +420,23 @@ __global__ void __launch_bounds__(256) rr_gemm_kernel(rr_gemm_t g0, rr_gemm_t g1
     }
 }
 
-// FP64 cyclic Jacobi on the c x c matrix M (ld c) with eigenvectors in V,
-// all threads of the block; returns 1 when converged.
-__device__ int rr_jacobi64(double* M, double* V, int c)
+// FP64 cyclic Jacobi on the c x c matrix M (leading dimension lm); V (same
+// layout) receives the eigenvectors as columns.  All threads of the block.
+__device__ int rr_jacobi64(double* M, double* V, int c, int lm)
 {
   __shared__ double j_c[256], j_s[256];
   __shared__ int j_p[256], j_q[256];
   __shared__ int j_done;
   __shared__ double j_red[RR_THREADS];
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < c * c; e += nt) V[e] = (e % c == e / c) ? 1.0 : 0.0;
+  // V^T is accumulated (row r of V^T = column r of V) so that the generic
+  // rounds rotate its columns; transposed back at the end
+  for (int e = tid; e < c * c; e += nt) V[(e % c) + (e / c) * lm] = (e % c == e / c) ? 1.0 : 0.0;
   double acc = 0.0;
-  for (int e = tid; e < c * c; e += nt) acc += M[e] * M[e];
+  for (int e = tid; e < c * c; e += nt) {
+    double v = M[(e % c) + (e / c) * lm];
+    acc += v * v;
+  }
   j_red[tid] = acc;
   __syncthreads();
   for (int o = nt / 2; o > 0; o >>= 1) {
@@ -348,75 +444,30 @@ __device__ int rr_jacobi64(double* M, double* V, int c)
     __syncthreads();
   }
   const double nrm = sqrt(j_red[0]);
-  const double thr_rot = 1e-3 * DBL_EPSILON * nrm, thr_done = 4.0 * DBL_EPSILON * nrm;
-  const int me = (c + 1) & ~1, half = me / 2;
-  int converged = 0;
-  for (int sweep = 0; sweep < JACOBI64_MAX_SWEEPS && !converged; sweep++) {
-    if (tid == 0) j_done = 1;
-    __syncthreads();
-    for (int round = 0; round < me - 1; round++) {
-      for (int t = tid; t < half; t += nt) {
-        int p, q;
-        rr_pair(t, round, me, &p, &q);
-        double cs = 1.0, sn = 0.0;
-        if (q < c) {
-          double apq = M[p + q * c], app = M[p + p * c], aqq = M[q + q * c];
-          if (fabs(apq) > thr_rot) {
-            double theta = (aqq - app) / (2.0 * apq);
-            double tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-            cs = 1.0 / sqrt(1.0 + tt * tt);
-            sn = tt * cs;
-            if (fabs(apq) > thr_done) j_done = 0;
-          }
-        }
-        j_p[t] = p;
-        j_q[t] = q;
-        j_c[t] = cs;
-        j_s[t] = sn;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * c; e += nt) {
-        int t = e / c, j = e % c;
-        double sn = j_s[t];
-        if (sn == 0.0) continue;
-        int p = j_p[t], q = j_q[t];
-        double cs = j_c[t];
-        double ap = M[p + j * c], aq = M[q + j * c];
-        M[p + j * c] = cs * ap - sn * aq;
-        M[q + j * c] = sn * ap + cs * aq;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * c; e += nt) {
-        int t = e / c, i = e % c;
-        double sn = j_s[t];
-        if (sn == 0.0) continue;
-        int p = j_p[t], q = j_q[t];
-        double cs = j_c[t];
-        double ap = M[i + p * c], aq = M[i + q * c];
-        M[i + p * c] = cs * ap - sn * aq;
-        M[i + q * c] = sn * ap + cs * aq;
-        double vp = V[i + p * c], vq = V[i + q * c];
-        V[i + p * c] = cs * vp - sn * vq;
-        V[i + q * c] = sn * vp + cs * vq;
-      }
-      __syncthreads();
-      for (int t = tid; t < half; t += nt)
-        if (j_s[t] != 0.0) {
-          M[j_p[t] + j_q[t] * c] = 0.0;
-          M[j_q[t] + j_p[t] * c] = 0.0;
-        }
-      __syncthreads();
+  int sweeps = 0;
+  int ok = rr_jacobi_rounds<double>(M, c, lm, V, c, lm, 1e-3 * DBL_EPSILON * nrm,
+                                    4.0 * DBL_EPSILON * nrm, JACOBI64_MAX_SWEEPS, j_c, j_s, j_p,
+                                    j_q, &j_done, &sweeps);
+  // V holds V^T row-wise: V[r*lm + j] = (V^T)_{r j} = V_{j r}; make it V_{i r} at [i + r*lm]
+  for (int e = tid; e < c * c; e += nt) {
+    int i = e % c, r = e / c;
+    if (i < r) {
+      double a = V[i + r * lm], b = V[r + i * lm];
+      V[i + r * lm] = b;
+      V[r + i * lm] = a;
     }
-    converged = j_done;
-    __syncthreads();
   }
-  return converged;
+  __syncthreads();
+  return ok;
 }
 
 // refinement step: S = X'AX, P = X'BX -> EI = I + E, Q (block diagonal on
 // the clusters), lam
+#define RR_CLUSTER_SMEM 96
+
 __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch s, int last)
 {
+  extern __shared__ double csm[];  // 2 x RR_CLUSTER_SMEM x rr_pad(RR_CLUSTER_SMEM)
   __shared__ double lt[512];
   __shared__ int cstart[513];
   __shared__ int ncl;
@@ -435,7 +486,9 @@ __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch
     if (tid < o) s_red[tid] = fmax(s_red[tid], s_red[tid + o]);
     __syncthreads();
   }
-  const double delta = 1e-3 * s_red[0] + 1e-300;
+  // close values are refined together: the first-order correction of a pair
+  // is (FP32 error ~1e-7 |C|) / gap, kept below ~1e-2
+  const double delta = 2e-5 * s_red[0] + 1e-300;
   if (tid == 0) {
     int n = 0;
     cstart[n++] = 0;
@@ -483,31 +536,43 @@ __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch
   for (int c = 0; c < ncl; c++) {
     const int a0 = cstart[c], sz = cstart[c + 1] - a0;
     if (sz < 2) continue;
-    double* Mc = s.J1;
-    double* Vc = s.J2;
+    if (tid == 0) atomicMax(&s.count[1], sz);
+    const int small = sz <= RR_CLUSTER_SMEM;
+    const int lm = small ? rr_pad(sz) : sz;
+    double* Mc = small ? csm : s.J1;
+    double* Vc = small ? csm + RR_CLUSTER_SMEM * rr_pad(RR_CLUSTER_SMEM) : s.J2;
+    // M_c = S + (R S + S R)/2 with R = I - P:  M_c = 2S - (P S + (P S)')/2,
+    // S, P symmetric; P S staged through the eigenvector buffer
     for (int e = tid; e < sz * sz; e += nt) {
       int a = e % sz, b = e / sz;
-      double v = S[(a0 + a) + (size_t)(a0 + b) * m];
+      Mc[a + b * lm] = S[(a0 + a) + (size_t)(a0 + b) * m];
+      Vc[a + b * lm] = P[(a0 + a) + (size_t)(a0 + b) * m];
+    }
+    __syncthreads();
+    double* PS = s.F;  // sz x sz, leading dimension sz (F is written only later)
+    for (int e = tid; e < sz * sz; e += nt) {
+      int a = e % sz, b = e / sz;
       double t = 0.0;
-      for (int l = 0; l < sz; l++) {
-        double ral = (a == l ? 1.0 : 0.0) - P[(a0 + a) + (size_t)(a0 + l) * m];
-        double rlb = (l == b ? 1.0 : 0.0) - P[(a0 + l) + (size_t)(a0 + b) * m];
-        t += ral * S[(a0 + l) + (size_t)(a0 + b) * m] + S[(a0 + a) + (size_t)(a0 + l) * m] * rlb;
-      }
-      Mc[a + b * sz] = v + 0.5 * t;
+      for (int l = 0; l < sz; l++) t += Vc[a + l * lm] * Mc[l + b * lm];
+      PS[a + b * sz] = t;
+    }
+    __syncthreads();
+    for (int e = tid; e < sz * sz; e += nt) {
+      int a = e % sz, b = e / sz;
+      Mc[a + b * lm] = 2.0 * Mc[a + b * lm] - 0.5 * (PS[a + b * sz] + PS[b + a * sz]);
     }
     __syncthreads();
     // symmetrise
     for (int e = tid; e < sz * sz; e += nt) {
       int a = e % sz, b = e / sz;
       if (a > b) {
-        double v = 0.5 * (Mc[a + b * sz] + Mc[b + a * sz]);
-        Mc[a + b * sz] = v;
-        Mc[b + a * sz] = v;
+        double v = 0.5 * (Mc[a + b * lm] + Mc[b + a * lm]);
+        Mc[a + b * lm] = v;
+        Mc[b + a * lm] = v;
       }
     }
     __syncthreads();
-    int ok = rr_jacobi64(Mc, Vc, sz);
+    int ok = rr_jacobi64(Mc, Vc, sz, lm);
     if (!ok) {
       if (tid == 0) s.status[0] = 3;
       return;
@@ -515,10 +580,10 @@ __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch
     // ascending order inside the cluster
     __shared__ int cperm[512];
     for (int a = tid; a < sz; a += nt) {
-      double da = Mc[a + a * sz];
+      double da = Mc[a + a * lm];
       int r = 0;
       for (int b = 0; b < sz; b++) {
-        double db = Mc[b + b * sz];
+        double db = Mc[b + b * lm];
         if (db < da || (db == da && b < a)) r++;
       }
       cperm[r] = a;
@@ -526,20 +591,16 @@ __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch
     __syncthreads();
     for (int e = tid; e < sz * sz; e += nt) {
       int a = e % sz, r = e / sz;
-      s.Q[(a0 + a) + (size_t)(a0 + r) * m] = Vc[a + cperm[r] * sz];
+      s.Q[(a0 + a) + (size_t)(a0 + r) * m] = Vc[a + cperm[r] * lm];
     }
-    for (int r = tid; r < sz; r += nt) s.lam[a0 + r] = Mc[cperm[r] + cperm[r] * sz];
+    for (int r = tid; r < sz; r += nt) s.lam[a0 + r] = Mc[cperm[r] + cperm[r] * lm];
     __syncthreads();
   }
 }
 
-__global__ void rr_finish_kernel(int m, rr_scratch s, double* A, int ld, double* w, int* info)
+__global__ void rr_finish_kernel(int m, rr_scratch s, double* w, int* info)
 {
   if (s.status[0]) return;  // the FP64 fallback writes the outputs
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * m; e += gridDim.x * blockDim.x) {
-    int i = e % m, j = e / m;
-    A[i + (size_t)j * ld] = s.X[e];
-  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
     w[i] = s.lam[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) *info = 0;
@@ -557,9 +618,9 @@ extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, do
     return gb_sygv_fp64(ctx, A, B, ld, m, w, info, NULL, forced);
 
   const size_t mm = (size_t)m * m;
-  size_t bytes = 4 * mm * sizeof(float) + 512 * sizeof(float) + 13 * mm * sizeof(double) +
-                 512 * sizeof(double) + 64;
-  char* base = (char*)gb_workspace(ctx, bytes + 1024);
+  size_t bytes = 2 * mm * sizeof(float) + 512 * sizeof(float) + 16 * mm * sizeof(double) +
+                 512 * sizeof(double) + 64 + 20 * 256;
+  char* base = (char*)gb_workspace(ctx, bytes);
   if (!base) return -1;
   rr_scratch s;
   size_t off = 0;
@@ -568,15 +629,16 @@ extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, do
     off += (b + 255) / 256 * 256;
     return p;
   };
-  s.L = (float*)take(mm * 4);
   s.C = (float*)take(mm * 4);
-  s.W = (float*)take(mm * 4);
   s.V = (float*)take(mm * 4);
   s.lam32 = (float*)take(512 * 4);
+  s.L64 = (double*)take(mm * 8);
+  s.LT64 = (double*)take(mm * 8);
+  s.C64 = (double*)take(mm * 8);
+  s.W64 = (double*)take(mm * 8);
   s.X = (double*)take(mm * 8);
   s.Xn = (double*)take(mm * 8);
   s.TA = (double*)take(mm * 8);
-  s.TB = (double*)take(mm * 8);
   s.S = (double*)take(mm * 8);
   s.P = (double*)take(mm * 8);
   s.EI = (double*)take(mm * 8);
@@ -586,45 +648,57 @@ extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, do
   s.J2 = (double*)take(mm * 8);
   s.lam = (double*)take(512 * 8);
   s.status = (int*)take(64);
+  s.count = ctx->dcount;
 
   cudaStream_t st = S_(ctx);
-  gb_prof_rec pr;
+  gb_prof_rec pr, ps;
   gb_prof_begin(ctx, &pr, GB_K_SYGV);
-  const size_t sm_red = mm * sizeof(float);
-  cudaFuncSetAttribute(rr_reduce32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_red);
-  rr_reduce32_kernel<<<1, RR_THREADS, sm_red, st>>>(A, B, ld, m, s);
+  const double m3 = (double)m * m * m;
+#define RR_STAGE(cls, flops, launch) \
+  gb_prof_begin(ctx, &ps, cls);      \
+  launch;                            \
+  gb_prof_end(ctx, &ps, 8.0 * m * m, flops)
+  const unsigned tb = (unsigned)((m + 7) / 8);  // 8 warps (columns) per CTA
+  RR_STAGE(GB_K_RR_CHOL, m3 / 3, (rr_chol64_kernel<<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(0, A, ld, s.W64, m, m, s)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(1, s.W64, m, s.C64, m, m, s)));
+  rr_sym_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
+  rr_sym_store_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
   // Jacobi: every CTA holds C (m*m) and `rows` rows of V
   const int nsplit = m <= 96 ? 1 : 4;
   const int rows = (m + nsplit - 1) / nsplit;
-  const size_t sm_jac = (mm + (size_t)rows * m) * sizeof(float);
+  const size_t sm_jac = ((size_t)m * rr_pad(m) + (size_t)rows * rr_pad(m)) * sizeof(float);
   cudaFuncSetAttribute(rr_jacobi32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_jac);
-  rr_jacobi32_kernel<<<nsplit, RR_THREADS, sm_jac, st>>>(m, rows, s);
-  cudaFuncSetAttribute(rr_backsub32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_red);
-  rr_backsub32_kernel<<<1, RR_THREADS, sm_red, st>>>(m, s);
-  int launches = 3;
-  const dim3 gg((m + 31) / 32, (m + 31) / 32, 2), g1((m + 31) / 32, (m + 31) / 32, 1);
+  RR_STAGE(GB_K_RR_JAC32, 0.0, (rr_jacobi32_kernel<<<nsplit, RR_THREADS, sm_jac, st>>>(m, rows, s)));
+  rr_vsort_kernel<<<1, RR_THREADS, 0, st>>>(m, s);
+  int launches = 7;
+  const size_t sm_ref = 2 * sizeof(double) * RR_CLUSTER_SMEM * rr_pad(RR_CLUSTER_SMEM);
+  cudaFuncSetAttribute(rr_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_ref);
+  const dim3 g1((m + 31) / 32, (m + 31) / 32, 1), g2((m + 31) / 32, (m + 31) / 32, 2);
   for (int round = 0; round < 2; round++) {
-    rr_gemm_t ta = {A, ld, 2, s.X, m, s.TA, m, m, m, m};
-    rr_gemm_t tb = {B, ld, 2, s.X, m, s.TB, m, m, m, m};
-    rr_gemm_kernel<<<gg, 256, 0, st>>>(ta, tb, s.status);
-    rr_gemm_t sa = {s.X, m, 1, s.TA, m, s.S, m, m, m, m};
-    rr_gemm_t sb = {s.X, m, 1, s.TB, m, s.P, m, m, m, m};
-    rr_gemm_kernel<<<gg, 256, 0, st>>>(sa, sb, s.status);
-    rr_refine_kernel<<<1, RR_THREADS, 0, st>>>(m, s, round == 1);
+    rr_gemm_t ta = {s.C64, m, 0, s.X, m, s.TA, m, m, m, m};  // C X
+    RR_STAGE(GB_K_RR_GEMM, 2 * m3, (rr_gemm_kernel<<<g1, 256, 0, st>>>(ta, ta, s.status)));
+    rr_gemm_t sa = {s.X, m, 1, s.TA, m, s.S, m, m, m, m};  // X' C X
+    rr_gemm_t sb = {s.X, m, 1, s.X, m, s.P, m, m, m, m};   // X' X
+    RR_STAGE(GB_K_RR_GEMM, 4 * m3, (rr_gemm_kernel<<<g2, 256, 0, st>>>(sa, sb, s.status)));
+    RR_STAGE(GB_K_RR_REFINE, 0.0, (rr_refine_kernel<<<1, RR_THREADS, sm_ref, st>>>(m, s, round == 1)));
     rr_gemm_t fq = {s.EI, m, 0, s.Q, m, s.F, m, m, m, m};
-    rr_gemm_kernel<<<g1, 256, 0, st>>>(fq, fq, s.status);
+    RR_STAGE(GB_K_RR_GEMM, 2 * m3, (rr_gemm_kernel<<<g1, 256, 0, st>>>(fq, fq, s.status)));
     rr_gemm_t xf = {s.X, m, 0, s.F, m, s.Xn, m, m, m, m};
-    rr_gemm_kernel<<<g1, 256, 0, st>>>(xf, xf, s.status);
+    RR_STAGE(GB_K_RR_GEMM, 2 * m3, (rr_gemm_kernel<<<g1, 256, 0, st>>>(xf, xf, s.status)));
     double* t = s.X;
     s.X = s.Xn;
     s.Xn = t;
     launches += 5;
   }
-  rr_finish_kernel<<<(m * m + 255) / 256, 256, 0, st>>>(m, s, A, ld, w, info);
-  launches++;
-  gb_prof_end(ctx, &pr, 32.0 * m * m, 2.0 * 2.0 * 5.0 * (double)m * m * m);
+  // eigenvectors of the pencil: inv(L)' X into A; values into w
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(2, s.X, m, A, ld, m, s)));
+  rr_finish_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(m, s, w, info);
+#undef RR_STAGE
+  launches += 2;
+  gb_prof_end(ctx, &pr, 32.0 * m * m, 16.0 * m3);
   gb_count_launch(launches);
   if (gb_cuda_check(ctx, (int)cudaGetLastError(), "rayleigh_ritz")) return -1;
-  // FP64 Jacobi on the original pencil when the FP32 stage failed
+  // FP64 Jacobi on the original pencil when the fast path did not finish
   return gb_sygv_fp64(ctx, A, B, ld, m, w, info, s.status, 0);
 }

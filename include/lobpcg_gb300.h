@@ -35,8 +35,8 @@ typedef struct {
   int precision;            /* LOBPCG_GPU_FP64 (default) or LOBPCG_GPU_MIXED */
   double compensated_below; /* mixed: hi+lo compensated Gram once max residual < this (1e-6) */
   double fp64_below;        /* mixed: continue in FP64 once max residual < this (2e-6) */
-  int fp32_stall;           /* mixed: also switch after this many FP32 iterations without
-                               progress of the max residual (10) */
+  int fp32_stall;           /* mixed: also switch after this many FP32 iterations without a
+                               new minimum of the largest active residual (20) */
   int tensor_cores;         /* mixed: 1 = tcgen05 TF32 kernels, 0 = FP32 CUDA-core kernels */
   int potrf_fail_at;        /* tests: the Nth Cholesky reports INFO = 1 (0 = off) */
   int sygv_fail_at;         /* tests: the Nth Rayleigh-Ritz solve reports INFO = 1 (0 = off) */
@@ -53,6 +53,10 @@ typedef struct {
   double seconds_fp32;
   double seconds_fp64;
   double final_max_residual;
+  int rr_calls;             /* Rayleigh-Ritz solves of the last solve */
+  int rr_jacobi32_sweeps;   /* FP32 Jacobi sweeps summed over those solves */
+  int rr_max_cluster;       /* largest cluster of close Ritz values refined together */
+  int rr_fallbacks;         /* solves that fell back to the one-CTA FP64 Jacobi */
 } lobpcg_gpu_stats;
 
 /* per-kernel-class timing, collected with CUDA events on the context's
@@ -150,6 +154,19 @@ int gpu_OperatorDiagonal(gpu_Operator* op, double* host_diag);
 void gpu_OperatorDestroy(gpu_Operator* op);
 /* the callback to pass as operatorA/B/T together with the gpu_Operator* */
 void gpu_OperatorApply(void* op, void* X, void* Y);
+
+/* The two Gram matrices of an explicit-Gram LOBPCG step on the active
+   columns of the blocks: G = [X R P]'[AX AR AP], H = [X R P]'[X R P], m x m
+   (m = widths of X + R + P; R/P and AR/AP may be NULL), written to host
+   column-major arrays with leading dimension ldh.  mode 0: CUDA-core kernel
+   (FP64 or FP32 blocks); mode 1: tensor cores, TF32 products with FP32
+   accumulation; mode 2: tensor cores, compensated 3xTF32 (hi*hi + hi*lo +
+   lo*hi); modes 1-2 take FP32 blocks with X at most 64 columns and R, P at
+   most 32 (X <= 32) or 64 columns.  No counterpart in the reference, whose
+   solver forms these blocks one pair at a time (lobpcg.c:1092-1160). */
+int gpu_ExplicitGram(gpu_MultiVector* X, gpu_MultiVector* R, gpu_MultiVector* P,
+                     gpu_MultiVector* AX, gpu_MultiVector* AR, gpu_MultiVector* AP, int mode,
+                     double* G_host, double* H_host, int ldh);
 
 /* ---------------------------------------------------------------- */
 /* Gram product without any allocation                               */

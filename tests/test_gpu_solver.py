@@ -121,18 +121,23 @@ def test_stencil_operator_solve_matches_csr(ctx):
     parity.check(g, r.flag, r.iterations, r.lam)
 
 
+@pytest.mark.parametrize("tensor_cores", [1, 0])
 @pytest.mark.parametrize("name", ["lap20_k10_maxit1000", "st7vc_12_k6_jacobi", "gen27_8_k4",
                                   "constraints_diag40", "serial_driver"])
-def test_mixed_precision_meets_tolerance(ctx, name):
-    """Mixed mode: FP32 iterations, then FP64 to the requested tolerance.
-    Eigenvalues against the reference within 1e-10 relative."""
+def test_mixed_precision_meets_tolerance(ctx, name, tensor_cores):
+    """Mixed mode: FP32 iterations (Gram products on the tensor cores or on
+    the CUDA cores), then FP64 to the requested tolerance.  Eigenvalues
+    against the reference within 1e-10 relative."""
     g = load(name)
     case = C.build(name)
-    ctx.set_options(precision=S.MIXED)
+    # the FP32 -> FP64 hand-over restarts the recurrence (P is dropped), so a
+    # slowly converging case may need a few more iterations than in FP64
+    case.maxit *= 3
+    ctx.set_options(precision=S.MIXED, tensor_cores=tensor_cores)
     try:
         r, x = run_case(ctx, case)
     finally:
-        ctx.set_options(precision=S.FP64)
+        ctx.set_options(precision=S.FP64, tensor_cores=1)
     assert r.flag == 0, ctx.last_error()
     tol = np.abs(r.lam) * case.rtol + case.atol + np.finfo(float).eps
     assert np.all(r.res <= tol)
