@@ -27,7 +27,7 @@ class BlasLapack(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("compensated_below", c_double), ("fp64_below", c_double),
                 ("fp32_stall", c_int), ("tensor_cores", c_int), ("potrf_fail_at", c_int),
-                ("sygv_fail_at", c_int), ("rr_fp64_only", c_int)]
+                ("sygv_fail_at", c_int), ("rr_method", c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -36,7 +36,8 @@ class Stats(ctypes.Structure):
                 ("seconds_total", c_double), ("seconds_fp32", c_double),
                 ("seconds_fp64", c_double), ("final_max_residual", c_double),
                 ("rr_calls", c_int), ("rr_jacobi32_sweeps", c_int), ("rr_max_cluster", c_int),
-                ("rr_fallbacks", c_int)]
+                ("rr_fallbacks", c_int), ("rr_graded", c_int),
+                ("explicit_undos", c_int)]
 
 
 class KernelTime(ctypes.Structure):

@@ -14,7 +14,8 @@ static const char* k_names[GB_K_COUNT] = {"gram", "xc_update", "spmm_csr", "sten
                                           "stencil5", "stencil27", "diag_scale", "residual",
                                           "blas1", "cholqr", "sygv", "small_dense", "tc_gram",
                                           "tc_xc_update", "sygv_fp64_gate", "rr_chol64",
-                                          "rr_trsm64", "rr_jacobi32", "rr_gemm64", "rr_refine"};
+                                          "rr_trsm64", "rr_jacobi32", "rr_gemm64", "rr_refine",
+                                          "rr_tridiag", "rr_tridiag_eig"};
 
 
 extern "C" void gb_count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }

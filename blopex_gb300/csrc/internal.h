@@ -25,7 +25,8 @@ typedef struct {
 enum {
   GB_K_GRAM = 0, GB_K_XC, GB_K_CSR, GB_K_ST7, GB_K_ST5, GB_K_ST27, GB_K_DIAG, GB_K_RESID,
   GB_K_BLAS1, GB_K_CHOLQR, GB_K_SYGV, GB_K_SMALL, GB_K_TC_GRAM, GB_K_TC_XC, GB_K_SYGV_FALLBACK,
-  GB_K_RR_CHOL, GB_K_RR_TRSM, GB_K_RR_JAC32, GB_K_RR_GEMM, GB_K_RR_REFINE, GB_K_COUNT
+  GB_K_RR_CHOL, GB_K_RR_TRSM, GB_K_RR_JAC32, GB_K_RR_GEMM, GB_K_RR_REFINE, GB_K_RR_TRID,
+  GB_K_RR_EIG, GB_K_COUNT
 };
 
 typedef struct {
@@ -133,7 +134,11 @@ int gb_cholqr_factor(gpu_Context* ctx, double* A, int ld, int m, int* info);
 /* generalized symmetric-definite eigenproblem A v = w B v (itype 1, lower
    triangles read): A <- eigenvectors (B-orthonormal, ascending), w <- values,
    B <- its lower Cholesky factor; *info as dsygv */
-int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w, int* info);
+/* Rayleigh-Ritz: lowest nev eigenpairs of A v = w B v into A's first nev
+   columns and w; INFO as dsygv.  B is reported as not definite (INFO m+j)
+   when a Cholesky pivot ratio L_jj^2 / B_jj falls below report_below. */
+int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, int nev, double* w, int* info,
+            double report_below);
 /* small helpers on device matrices */
 int gb_small_symmetrize(gpu_Context* ctx, double* A, int ld, int m);
 int gb_small_identity(gpu_Context* ctx, double* A, int ld, int h, int w);

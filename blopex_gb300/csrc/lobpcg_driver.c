@@ -196,7 +196,7 @@ static int d_implicit_qr(solver_t* s, gpu_MultiVector* x, gpu_MultiVector* bx, d
 
 static int d_sygv(solver_t* s, int m, double* w, int* info)
 {
-  if (gb_sygv(s->ctx, s->gA, s->gB, s->k3, m, w, s->info)) return -1;
+  if (gb_sygv(s->ctx, s->gA, s->gB, s->k3, m, s->k, w, s->info, 0.0)) return -1;
   return read_info(s, info);
 }
 
@@ -566,6 +566,13 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
 
 /* ------------------------------------------------- explicit-Gram phase */
 
+/* the FP32 Gram matrices carry relative errors down to ~1e-6 (compensated)
+   and ~1e-4 (TF32): a basis vector whose squared sine to the span of the
+   previous ones is below this is not resolved, and P is dropped */
+#define EXPLICIT_PIVOT_BELOW 1e-6
+/* a step whose largest active residual grows by more than this is undone */
+#define EXPLICIT_JUMP 20.0
+
 static size_t dt_size(int dtype) { return dtype == GPU_MV_FLOAT64 ? 8 : 4; }
 
 /* column table entries for columns idx[0..n) of x, appended at offset */
@@ -652,7 +659,8 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
   const int k = s->k, k3 = s->k3;
   int* it = ctl->iteration;
   int act[BLK_MAXCOLS], prev_act[BLK_MAXCOLS];
-  int nR = k, prev_nR = k, nP = 0, haveP = 0;
+  int nR = k, prev_nR = k, nP = 0, haveP = 0, prev_haveP = 0;
+  double prev_lam[BLK_MAXCOLS], prev_norm[BLK_MAXCOLS];
   double best = HUGE_VAL;
   int stall = 0;
   gpu_MultiVector *X = s->X, *AX = s->AX, *BX = s->noB ? X : s->BX;
@@ -785,7 +793,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         if (gb_small_copy(s->ctx, eb->G2, k3, eb->Gs, k3, mm, mm) ||
             gb_small_copy(s->ctx, eb->H2, k3, eb->Hs, k3, mm, mm))
           return -2;
-        if (gb_sygv(s->ctx, eb->Gs, eb->Hs, k3, mm, eb->w, s->info) || read_info(s, &info))
+        if (gb_sygv(s->ctx, eb->Gs, eb->Hs, k3, mm, k, eb->w, s->info, EXPLICIT_PIVOT_BELOW) || read_info(s, &info))
           return -2;
         if (info == 0 || use_p == 0) break;
         use_p = 0;
@@ -800,6 +808,8 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       /* coordinates in the original basis: C = T C' (first k columns) */
       if (gb_small_gemm(s->ctx, eb->T, k3, 0, eb->Gs, k3, 0, eb->tmp, k3, mm, k, mm)) return -2;
       if (gb_small_copy(s->ctx, eb->tmp, k3, eb->Gs, k3, mm, k)) return -2;
+      /* keep the previous Ritz values for an undo (eb->d) */
+      if (gb_memcpy_d2d(s->ctx, eb->d, s->lam, sizeof(double) * k)) return -2;
       if (gb_memcpy_d2d(s->ctx, s->lam, eb->w, sizeof(double) * k)) return -2;
 
       /* P = [R P(act)] C_RP ; X = X C_X + P, and the A / B images */
@@ -834,18 +844,60 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         BP = P;
         BPn = Pn;
       }
+      prev_haveP = haveP;
       haveP = 1; /* P holds all k columns from now on */
     }
 
     /* residuals of the active columns and the new Ritz values */
+    memcpy(prev_lam, s->h_lam, sizeof(double) * k);
+    memcpy(prev_norm, s->h_norm, sizeof(double) * k);
     if (fetch_lambda(s)) return -2;
-    if (nonfinite(s->h_lam, k)) {
-      ctl->handed_over = 1;
-      break;
+    int undo = nonfinite(s->h_lam, k);
+    if (!undo) {
+      if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
+      /* A Ritz pair of the FP32 pencil that is not one of the operator
+         (Gram errors ~1e-4 with TF32 products) shows as a jump of the
+         largest residual: undo the step -- the previous block, its images
+         and P are intact in the other buffers -- and continue with more
+         precise products (TF32 -> compensated -> FP64). */
+      double mo = 0.0, mn = 0.0;
+      for (int c = 0; c < nR; c++) {
+        mo = fmax(mo, prev_norm[act[c]]);
+        mn = fmax(mn, s->h_norm[act[c]]);
+      }
+      undo = !(mn <= EXPLICIT_JUMP * mo);
     }
-    if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
-    prev_nR = nR;
-    memcpy(prev_act, act, sizeof(int) * nR);
+    if (undo) {
+      gpu_MultiVector* t;
+      t = X; X = Xn; Xn = t;
+      t = AX; AX = AXn; AXn = t;
+      t = P; P = Pn; Pn = t;
+      t = AP; AP = APn; APn = t;
+      if (!s->noB) {
+        t = BX; BX = BXn; BXn = t;
+        t = BP; BP = BPn; BPn = t;
+      } else {
+        BX = X;
+        BXn = Xn;
+        BP = P;
+        BPn = Pn;
+      }
+      haveP = prev_haveP;
+      memcpy(s->h_lam, prev_lam, sizeof(double) * k);
+      memcpy(s->h_norm, prev_norm, sizeof(double) * k);
+      if (gb_memcpy_d2d(s->ctx, s->lam, eb->d, sizeof(double) * k)) return -2;
+      s->ctx->stats.explicit_undos++;
+      if (!tc_ok || comp) {
+        ctl->handed_over = 1;
+        break;
+      }
+      comp = 1;
+      stall = 0;
+      prev_nR = -1; /* R holds the rejected step's residual: recompute */
+    } else {
+      prev_nR = nR;
+      memcpy(prev_act, act, sizeof(int) * nR);
+    }
     {
       const int col = *it;
       if (ctl->lam_hist && col <= ctl->maxit)
@@ -1149,6 +1201,7 @@ done:
       ctx->stats.rr_max_cluster = c[1];
       ctx->stats.rr_fallbacks = c[2];
       ctx->stats.rr_calls = c[3];
+      ctx->stats.rr_graded = c[4];
     }
   }
   ctx->stats.seconds_total = gb_now() - t0;

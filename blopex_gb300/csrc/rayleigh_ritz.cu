@@ -1,30 +1,36 @@
 // rayleigh_ritz.cu -- the Rayleigh-Ritz eigenproblem A v = w B v (B SPD,
 // order m <= 3k) of every LOBPCG iteration, replacing the dsygv call of
-// lobpcg_solveGEVP (blopex_abstract/krylov/lobpcg.c:66-103), built for a GPU
-// whose FP32 rate is 64 times its FP64 rate:
+// lobpcg_solveGEVP (blopex_abstract/krylov/lobpcg.c:66-103).  Only the
+// lowest nev (= k) eigenpairs are used by the caller and computed.
 //
-//   1. FP64, one CTA: Cholesky B = L L' (its failure is dsygv's INFO m+j)
-//   2. FP64, multi-CTA triangular solves: C = inv(L) A inv(L)'   -- the
-//      conditioning of B is handled here, in FP64, as dsygv does
-//   3. FP32, cyclic Jacobi on C; every CTA rotates its own copy of C
-//      (identical arithmetic, no communication) and accumulates its own
-//      slice of rows of the eigenvector matrix V
-//   4. FP64 refinement of V, twice: with S = V'CV and P = V'V
-//      (multi-CTA FP64 GEMMs), the Ritz values l_i = S_ii / P_ii and the
-//      correction V <- V (I + E),
-//        E_ij = (S_ij - l_j P_ij) / (l_j - l_i)   for separated pairs,
-//        E_ij = R_ij / 2 with R = I - P           inside clusters,
-//      and inside each cluster of close values the FP64 matrix
-//      S_cc + (R_cc S_cc + S_cc R_cc)/2 is diagonalised by FP64 Jacobi.
-//      This is the iterative refinement of Ogita & Aishima (symmetric
-//      eigenproblems, Japan J. Indust. Appl. Math. 2018); each round
-//      squares the eigenvector error.
-//   5. FP64, multi-CTA: eigenvectors of the pencil inv(L)' V into A, values
-//      into w (dsygv's outputs; B is left intact).
-// If the FP32 Jacobi does not converge or the refinement does not settle,
-// the one-CTA FP64 Jacobi solver of dense.cu runs on the original pencil
-// instead (gated on a device status word, no host sync).  Every loop has a
-// fixed trip count.
+// Default solver (rr_method 0), all FP64, the steps of dsygv:
+//   1. one CTA: Cholesky B = L L' (its failure is dsygv's INFO m+j)
+//   2. multi-CTA triangular solves: C = inv(L) A inv(L)'
+//   3. one CTA: Householder reduction C = Q T Q', T tridiagonal
+//   4. one warp per eigenvalue: multisection (32 Sturm counts per step)
+//      for the nev smallest eigenvalues of T
+//   5. one CTA per eigenvalue: inverse iteration on T - lambda I (LU with
+//      partial pivoting), then Cholesky-QR (twice) of the nev vectors --
+//      the vectors of near-degenerate eigenvalues come from different
+//      starts and are orthonormalised together
+//   6. one warp per vector: back-transformation by the Householder
+//      reflectors, then inv(L)' (dsygv's outputs; B is left intact).
+// The FP64 rate of this GPU is 1/64 of its FP32 rate; the one-CTA steps are
+// O(m^3) on one SM (about 1.5 ms at m = 192).
+//
+// rr_method 2, for well-separated spectra: FP32 cyclic Jacobi on C (every
+// CTA rotates its own copy and accumulates a slice of the eigenvectors),
+// then two rounds of FP64 refinement with S = V'CV and P = V'V,
+//   E_ij = (S_ij - l_j P_ij) / (l_j - l_i)   for separated pairs,
+//   E_ij = R_ij / 2 with R = I - P           inside clusters,
+// clusters diagonalised by FP64 Jacobi (Ogita & Aishima, Japan J. Indust.
+// Appl. Math. 2018: each round squares the eigenvector error).  Its FP32
+// start carries errors of eps32 |C| / gap, so it fails on pencils whose
+// wanted eigenvalues are close compared with |C|.
+//
+// Whenever a path cannot finish (status word), the one-CTA FP64 Jacobi
+// solver of dense.cu runs on the original pencil instead, gated on the
+// device status word (no host sync).  Every loop has a fixed trip count.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -34,7 +40,8 @@
 static inline cudaStream_t S_(gpu_Context* ctx) { return (cudaStream_t)ctx->stream; }
 
 #define RR_THREADS 1024
-#define RR_MAX_SMEM_M 192
+#define RR_MAX_SMEM_M 192  // FP32 Jacobi path (shared-memory copies of C)
+#define RR_MAX_M 384       // tridiagonal path
 #define JACOBI32_MAX_SWEEPS 30
 #define JACOBI64_MAX_SWEEPS 40
 
@@ -44,21 +51,34 @@ struct rr_scratch {
   float *C, *V, *lam32;
   double *L64, *LT64, *C64, *W64;
   double *X, *Xn, *TA, *S, *P, *EI, *Q, *F, *J1, *J2, *lam;
+  double *d, *e, *tau;  // tridiagonal T and the Householder scalars
   int* status;
 };
 
 // ------------------------------------------------------------------ 1.
 // FP64 lower Cholesky of B into s.L64 (m x m, ld m); *info = m + j on
 // failure (dsygv's convention for a B that is not positive definite).
+// The pivot ratio q_j = L_jj^2 / B_jj is the squared sine of the angle
+// between basis vector j and the span of the previous ones.  When its
+// minimum is below report_below, B is reported as not definite (INFO m+j,
+// so that the caller restarts without P); below RR_GRADED_BELOW, C is
+// graded beyond what the tridiagonal solver (absolute accuracy
+// eps |C|) resolves for the small eigenvalues, and the FP64 Jacobi solver
+// (relative accuracy on graded matrices) runs instead (status 7).
+#define RR_GRADED_BELOW 1e-10
 __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __restrict__ B, int ld,
-                                                               int m, rr_scratch s, int* info)
+                                                               int m, rr_scratch s, int* info,
+                                                               double report_below)
 {
   __shared__ int bad;
   double* L = s.L64;
   const int tid = threadIdx.x, nt = blockDim.x;
+  double qmin = HUGE_VAL;
+  int jmin = 0;
   if (tid == 0) {
     bad = 0;
     s.status[0] = 0;
+    atomicAdd(&s.count[3], 1);
   }
   for (int e = tid; e < m * m; e += nt) {
     int i = e % m, j = e / m;
@@ -68,10 +88,16 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
   for (int j = 0; j < m; j++) {
     if (tid == 0) {
       double d = L[j + (size_t)j * m];
-      if (!(d > 0.0) || !isfinite(d))
+      if (!(d > 0.0) || !isfinite(d)) {
         bad = j + 1;
-      else
+      } else {
         L[j + (size_t)j * m] = sqrt(d);
+        const double q = d / B[j + (size_t)j * ld];
+        if (q < qmin) {
+          qmin = q;
+          jmin = j;
+        }
+      }
     }
     __syncthreads();
     if (bad) break;
@@ -85,6 +111,15 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
     }
     __syncthreads();
   }
+  if (tid == 0 && !bad) {
+    if (qmin < report_below) {
+      bad = jmin + 1;
+    } else if (qmin < RR_GRADED_BELOW) {
+      s.status[0] = 7;
+      atomicAdd(&s.count[4], 1);
+    }
+  }
+  __syncthreads();
   if (bad) {
     if (tid == 0) {
       s.status[0] = 5;
@@ -105,15 +140,15 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
 //   mode 2: X = inv(L)' Y (Y m x m, ld ldy), result to X with leading dim ldx
 // s.LT holds L row-major (LT[p + i*m] = L(i, p)) so that the forward
 // sweeps read contiguous rows of L.
-#define RR_TRSM_SLOTS (RR_MAX_SMEM_M / 32)
+#define RR_TRSM_SLOTS (RR_MAX_M / 32)
 __global__ void __launch_bounds__(256) rr_trsm64_kernel(int mode, const double* __restrict__ Y,
                                                         int ldy, double* __restrict__ X, int ldx,
-                                                        int m, rr_scratch s)
+                                                        int m, int ncols, rr_scratch s)
 {
   if (s.status[0]) return;
   const int lane = threadIdx.x & 31;
   const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (j >= m) return;
+  if (j >= ncols) return;
   double xr[RR_TRSM_SLOTS];
 #pragma unroll
   for (int q = 0; q < RR_TRSM_SLOTS; q++) xr[q] = 0.0;
@@ -333,7 +368,6 @@ __global__ void __launch_bounds__(RR_THREADS) rr_jacobi32_kernel(int m, int rows
     if (tid == 0) {
       s.status[1] = sweeps;
       atomicAdd(&s.count[0], sweeps);
-      atomicAdd(&s.count[3], 1);
     }
   }
 }
@@ -598,72 +632,453 @@ __global__ void __launch_bounds__(RR_THREADS) rr_refine_kernel(int m, rr_scratch
   }
 }
 
-__global__ void rr_finish_kernel(int m, rr_scratch s, double* w, int* info)
+__global__ void rr_finish_kernel(int nev, rr_scratch s, double* w, int* info)
 {
   if (s.status[0]) return;  // the FP64 fallback writes the outputs
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nev; i += gridDim.x * blockDim.x)
     w[i] = s.lam[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) *info = 0;
+}
+
+// ------------------------------------------------------ tridiagonal path
+__device__ __forceinline__ double rr_warp_sum(double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide sum (all threads return it); red holds one double per warp
+__device__ double rr_block_sum(double v, double* red)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = rr_warp_sum(v);
+  __syncthreads();  // red may still be read by a previous call
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < nw; w++) t += red[w];
+  return t;
+}
+
+// 3. Householder reduction of the symmetric C (s.C64, lower triangle used,
+// ld m) to tridiagonal form, one CTA.  Step j reflects rows/columns j+1..m-1
+// with H_j = I - tau_j v v', v = (1, C[j+2.., j] / (alpha - beta)); v is
+// stored below the subdiagonal of column j.  Per step: p = tau A22 v in
+// two coalesced passes over the lower triangle (column sums, then row sums
+// of the strict part), w = p - (tau/2)(p'v) v, A22 -= v w' + w v'.
+#define RR_TRD_THREADS 512
+__global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_kernel(int m, rr_scratch s)
+{
+  __shared__ double v[RR_MAX_M], p[RR_MAX_M];
+  __shared__ double red[RR_TRD_THREADS / 32];
+  __shared__ double sh_tau, sh_scale;
+  if (s.status[0]) return;
+  double* A = s.C64;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = nt >> 5;
+  for (int j = 0; j + 2 < m; j++) {
+    const int n1 = m - j - 1;
+    double* col = A + (size_t)j * m + (j + 1);  // x = col[0 .. n1)
+    double acc = 0.0;
+    for (int i = 1 + tid; i < n1; i += nt) acc += col[i] * col[i];
+    acc = rr_block_sum(acc, red);
+    if (tid == 0) {
+      const double alpha = col[0];
+      double tau = 0.0, beta = alpha, scale = 0.0;
+      if (acc > 0.0) {
+        beta = -copysign(hypot(alpha, sqrt(acc)), alpha);
+        tau = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      s.d[j] = A[j + (size_t)j * m];
+      s.e[j] = beta;
+      s.tau[j] = tau;
+      sh_tau = tau;
+      sh_scale = scale;
+    }
+    __syncthreads();
+    const double tau = sh_tau, scale = sh_scale;
+    if (tau == 0.0) continue;  // uniform: x is already reduced
+    for (int i = tid; i < n1; i += nt) {
+      const double vi = (i == 0) ? 1.0 : col[i] * scale;
+      v[i] = vi;
+      if (i > 0) col[i] = vi;
+    }
+    __syncthreads();
+    double* A22 = A + (size_t)(j + 1) * m + (j + 1);  // (r, c) at A22[r + c*m]
+    // column part: p[c] = sum_{r >= c} A22(r, c) v[r]
+    for (int c = warp; c < n1; c += nw) {
+      const double* ac = A22 + (size_t)c * m;
+      double t = 0.0;
+      for (int r = c + lane; r < n1; r += 32) t += ac[r] * v[r];
+      t = rr_warp_sum(t);
+      if (lane == 0) p[c] = t;
+    }
+    __syncthreads();
+    // row part: + sum_{c < r} A22(r, c) v[c]; then p = tau * p
+    for (int r = tid; r < n1; r += nt) {
+      double t = 0.0;
+      for (int c = 0; c < r; c++) t += A22[r + (size_t)c * m] * v[c];
+      p[r] = tau * (p[r] + t);
+    }
+    __syncthreads();
+    acc = 0.0;
+    for (int i = tid; i < n1; i += nt) acc += p[i] * v[i];
+    const double K = 0.5 * tau * rr_block_sum(acc, red);
+    for (int i = tid; i < n1; i += nt) p[i] -= K * v[i];  // p <- w
+    __syncthreads();
+    for (int c = warp; c < n1; c += nw) {
+      double* ac = A22 + (size_t)c * m;
+      const double vc = v[c], wc = p[c];
+      for (int r = c + lane; r < n1; r += 32) ac[r] -= v[r] * wc + p[r] * vc;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (m >= 2) {
+      s.d[m - 2] = A[(m - 2) + (size_t)(m - 2) * m];
+      s.e[m - 2] = A[(m - 1) + (size_t)(m - 2) * m];
+      s.tau[m - 2] = 0.0;
+    }
+    s.d[m - 1] = A[(m - 1) + (size_t)(m - 1) * m];
+  }
+}
+
+// number of eigenvalues of T below x (Sturm count of the LDL' pivots)
+__device__ __forceinline__ int rr_sturm(const double* d, const double* e2, int m, double x,
+                                        double pivmin)
+{
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  int cnt = q < 0.0;
+  for (int i = 1; i < m; i++) {
+    q = (d[i] - x) - e2[i - 1] / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += q < 0.0;
+  }
+  return cnt;
+}
+
+// 4. eigenvalue j of T (ascending) by multisection: the 32 lanes count at
+// 31 interior points of [lo, hi]; the bracket shrinks 32-fold per step
+__global__ void __launch_bounds__(32) rr_bisect_kernel(int m, rr_scratch s)
+{
+  __shared__ double d[RR_MAX_M], e2[RR_MAX_M];
+  if (s.status[0]) return;
+  const int lane = threadIdx.x, j = blockIdx.x;
+  double emax2 = 0.0, glo = HUGE_VAL, ghi = -HUGE_VAL;
+  for (int i = lane; i < m; i += 32) {
+    const double di = s.d[i];
+    const double el = i > 0 ? fabs(s.e[i - 1]) : 0.0, er = i + 1 < m ? fabs(s.e[i]) : 0.0;
+    d[i] = di;
+    if (i + 1 < m) {
+      e2[i] = s.e[i] * s.e[i];
+      emax2 = fmax(emax2, e2[i]);
+    }
+    glo = fmin(glo, di - el - er);
+    ghi = fmax(ghi, di + el + er);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+    glo = fmin(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+    ghi = fmax(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+  }
+  __syncwarp();
+  const double pivmin = DBL_MIN * fmax(1.0, emax2);
+  const double tnorm = fmax(fabs(glo), fabs(ghi));
+  const double pad = 2.0 * DBL_EPSILON * tnorm * m + 2.0 * pivmin;
+  double lo = glo - pad, hi = ghi + pad;
+  for (int step = 0; step < 16; step++) {
+    if (hi - lo <= fmax(2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)), 0.25 * DBL_EPSILON * tnorm))
+      break;
+    const double x = (lane == 31) ? hi : lo + (hi - lo) * (double)(lane + 1) * (1.0 / 32.0);
+    const int cnt = (lane == 31) ? m : rr_sturm(d, e2, m, x, pivmin);
+    const unsigned ge = __ballot_sync(0xffffffffu, cnt >= j + 1);
+    const int f = __ffs(ge) - 1;  // first point with at least j+1 eigenvalues below it
+    const double xf = __shfl_sync(0xffffffffu, x, f);
+    const double xl = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+    hi = xf;
+    if (f > 0) lo = xl;
+  }
+  if (lane == 0) s.lam[j] = 0.5 * (lo + hi);
+}
+
+__device__ __forceinline__ double rr_start_value(int j, int i)
+{
+  unsigned long long z = 0x9E3779B97F4A7C15ull * (unsigned long long)(j * 1031 + i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+// 5. inverse iteration for eigenvalue j: Gaussian elimination with partial
+// pivoting of T - lambda I (upper factor with two superdiagonals), three
+// solves from a pseudo-random start; vector j into s.X (ld m)
+__global__ void __launch_bounds__(32) rr_invit_kernel(int m, rr_scratch s)
+{
+  __shared__ double u0i[RR_MAX_M], u1[RR_MAX_M], u2[RR_MAX_M], mu[RR_MAX_M], y[RR_MAX_M];
+  __shared__ unsigned char sw[RR_MAX_M];
+  __shared__ int bad;
+  if (s.status[0]) return;
+  const int lane = threadIdx.x, j = blockIdx.x;
+  const double lam = s.lam[j];
+  if (lane == 0) {
+    double tn = 0.0;
+    for (int i = 0; i < m; i++)
+      tn = fmax(tn, fabs(s.d[i]) + (i > 0 ? fabs(s.e[i - 1]) : 0.0) + (i + 1 < m ? fabs(s.e[i]) : 0.0));
+    const double tiny = DBL_EPSILON * fmax(tn, 1e-280);
+    double p0 = s.d[0] - lam, p1 = m > 1 ? s.e[0] : 0.0;
+    for (int k = 0; k + 1 < m; k++) {
+      const double b = s.e[k], a1 = s.d[k + 1] - lam, c1 = (k + 2 < m) ? s.e[k + 1] : 0.0;
+      if (fabs(p0) >= fabs(b)) {
+        if (fabs(p0) < tiny) p0 = p0 < 0.0 ? -tiny : tiny;
+        const double f = b / p0;
+        u0i[k] = 1.0 / p0;
+        u1[k] = p1;
+        u2[k] = 0.0;
+        mu[k] = f;
+        sw[k] = 0;
+        p0 = a1 - f * p1;
+        p1 = c1;
+      } else {
+        const double f = p0 / b;
+        u0i[k] = 1.0 / b;
+        u1[k] = a1;
+        u2[k] = c1;
+        mu[k] = f;
+        sw[k] = 1;
+        p0 = p1 - f * a1;
+        p1 = -f * c1;
+      }
+    }
+    if (fabs(p0) < tiny) p0 = p0 < 0.0 ? -tiny : tiny;
+    u0i[m - 1] = 1.0 / p0;
+    bad = 0;
+  }
+  for (int i = lane; i < m; i += 32) y[i] = rr_start_value(j, i);
+  for (int it = 0; it < 3; it++) {
+    __syncwarp();
+    if (lane == 0) {
+      for (int k = 0; k + 1 < m; k++) {
+        if (sw[k]) {
+          const double t = y[k];
+          y[k] = y[k + 1];
+          y[k + 1] = t - mu[k] * y[k];
+        } else {
+          y[k + 1] -= mu[k] * y[k];
+        }
+      }
+      y[m - 1] *= u0i[m - 1];
+      if (m > 1) y[m - 2] = (y[m - 2] - u1[m - 2] * y[m - 1]) * u0i[m - 2];
+      for (int k = m - 3; k >= 0; k--) y[k] = (y[k] - u1[k] * y[k + 1] - u2[k] * y[k + 2]) * u0i[k];
+    }
+    __syncwarp();
+    double mx = 0.0;
+    for (int i = lane; i < m; i += 32) mx = fmax(mx, fabs(y[i]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (!(mx > 0.0) || !isfinite(mx)) {
+      if (lane == 0) bad = 1;
+      break;
+    }
+    double ss = 0.0;
+    for (int i = lane; i < m; i += 32) {
+      const double t = y[i] / mx;
+      y[i] = t;
+      ss += t * t;
+    }
+    ss = rr_warp_sum(ss);
+    const double inv = 1.0 / sqrt(ss);
+    for (int i = lane; i < m; i += 32) y[i] *= inv;
+  }
+  __syncwarp();
+  if (bad) {
+    if (lane == 0) s.status[0] = 6;
+    return;
+  }
+  for (int i = lane; i < m; i += 32) s.X[i + (size_t)j * m] = y[i];
+}
+
+// Cholesky of the nev x nev Gram matrix s.S (upper, U'U = S) and U^-1 into
+// s.P; status 6 when the vectors are not numerically independent
+__global__ void __launch_bounds__(256) rr_cholinv_kernel(int nev, rr_scratch s)
+{
+  __shared__ int bad;
+  if (s.status[0]) return;
+  double* U = s.S;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < nev; j++) {
+    if (tid == 0) {
+      const double djj = U[j + (size_t)j * nev];
+      if (!(djj > 1e-6)) bad = 1;  // the vectors are unit vectors
+      else U[j + (size_t)j * nev] = sqrt(djj);
+    }
+    __syncthreads();
+    if (bad) break;
+    const double r = 1.0 / U[j + (size_t)j * nev];
+    for (int c = j + 1 + tid; c < nev; c += nt) U[j + (size_t)c * nev] *= r;
+    __syncthreads();
+    const int w = nev - j - 1;
+    for (int e = tid; e < w * w; e += nt) {
+      const int a = j + 1 + e % w, c = j + 1 + e / w;
+      if (a <= c) U[a + (size_t)c * nev] -= U[j + (size_t)a * nev] * U[j + (size_t)c * nev];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (tid == 0) s.status[0] = 6;
+    return;
+  }
+  // inverse of the upper factor, one thread per column
+  for (int c = tid; c < nev; c += nt) {
+    double* x = s.P + (size_t)c * nev;
+    for (int i = nev - 1; i > c; i--) x[i] = 0.0;
+    x[c] = 1.0 / U[c + (size_t)c * nev];
+    for (int i = c - 1; i >= 0; i--) {
+      double t = 0.0;
+      for (int l = i + 1; l <= c; l++) t += U[i + (size_t)l * nev] * x[l];
+      x[i] = -t / U[i + (size_t)i * nev];
+    }
+  }
+}
+
+// 6. z <- H_0 H_1 ... H_{m-3} z for the nev vectors of s.X, one warp per vector
+__global__ void __launch_bounds__(256) rr_backtr_kernel(int m, int nev, rr_scratch s)
+{
+  if (s.status[0]) return;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= nev) return;
+  double z[RR_TRSM_SLOTS];
+  double* zc = s.X + (size_t)j * m;
+#pragma unroll
+  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+    const int i = q * 32 + lane;
+    z[q] = i < m ? zc[i] : 0.0;
+  }
+  for (int h = m - 3; h >= 0; h--) {
+    const double tau = s.tau[h];
+    if (tau == 0.0) continue;
+    const double* vh = s.C64 + (size_t)h * m;  // v(h+1) = 1, v(i) = C[i, h] for i >= h+2
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+      const int i = q * 32 + lane;
+      if (i == h + 1)
+        t += z[q];
+      else if (i > h + 1 && i < m)
+        t += vh[i] * z[q];
+    }
+    t = tau * rr_warp_sum(t);
+#pragma unroll
+    for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+      const int i = q * 32 + lane;
+      if (i == h + 1)
+        z[q] -= t;
+      else if (i > h + 1 && i < m)
+        z[q] -= t * vh[i];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+    const int i = q * 32 + lane;
+    if (i < m) zc[i] = z[q];
+  }
 }
 
 // gated FP64 fallback (dense.cu)
 extern "C" int gb_sygv_fp64(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w,
                             int* info, const int* gate, int force);
 
-extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w, int* info)
+static char* rr_take(char* base, size_t* off, size_t b)
 {
-  ctx->sygv_calls++;
-  const int forced = ctx->opt.sygv_fail_at > 0 && ctx->sygv_calls == ctx->opt.sygv_fail_at;
-  if (forced || m > RR_MAX_SMEM_M || m < 2 || ctx->opt.rr_fp64_only)
-    return gb_sygv_fp64(ctx, A, B, ld, m, w, info, NULL, forced);
+  char* p = base + *off;
+  *off += (b + 255) / 256 * 256;
+  return p;
+}
 
+static int rr_scratch_setup(gpu_Context* ctx, int m, rr_scratch* s)
+{
   const size_t mm = (size_t)m * m;
-  size_t bytes = 2 * mm * sizeof(float) + 512 * sizeof(float) + 16 * mm * sizeof(double) +
-                 512 * sizeof(double) + 64 + 20 * 256;
+  const size_t bytes = 2 * mm * sizeof(float) + 512 * sizeof(float) + 16 * mm * sizeof(double) +
+                       4 * 512 * sizeof(double) + 64 + 24 * 256;
   char* base = (char*)gb_workspace(ctx, bytes);
   if (!base) return -1;
-  rr_scratch s;
   size_t off = 0;
-  auto take = [&](size_t b) {
-    char* p = base + off;
-    off += (b + 255) / 256 * 256;
-    return p;
-  };
-  s.C = (float*)take(mm * 4);
-  s.V = (float*)take(mm * 4);
-  s.lam32 = (float*)take(512 * 4);
-  s.L64 = (double*)take(mm * 8);
-  s.LT64 = (double*)take(mm * 8);
-  s.C64 = (double*)take(mm * 8);
-  s.W64 = (double*)take(mm * 8);
-  s.X = (double*)take(mm * 8);
-  s.Xn = (double*)take(mm * 8);
-  s.TA = (double*)take(mm * 8);
-  s.S = (double*)take(mm * 8);
-  s.P = (double*)take(mm * 8);
-  s.EI = (double*)take(mm * 8);
-  s.Q = (double*)take(mm * 8);
-  s.F = (double*)take(mm * 8);
-  s.J1 = (double*)take(mm * 8);
-  s.J2 = (double*)take(mm * 8);
-  s.lam = (double*)take(512 * 8);
-  s.status = (int*)take(64);
-  s.count = ctx->dcount;
+  s->C = (float*)rr_take(base, &off, mm * 4);
+  s->V = (float*)rr_take(base, &off, mm * 4);
+  s->lam32 = (float*)rr_take(base, &off, 512 * 4);
+  double** f64[] = {&s->L64, &s->LT64, &s->C64, &s->W64, &s->X, &s->Xn, &s->TA, &s->S,
+                    &s->P,   &s->EI,   &s->Q,   &s->F,   &s->J1, &s->J2};
+  for (size_t i = 0; i < sizeof(f64) / sizeof(f64[0]); i++) *f64[i] = (double*)rr_take(base, &off, mm * 8);
+  s->lam = (double*)rr_take(base, &off, 512 * 8);
+  s->d = (double*)rr_take(base, &off, 512 * 8);
+  s->e = (double*)rr_take(base, &off, 512 * 8);
+  s->tau = (double*)rr_take(base, &off, 512 * 8);
+  s->status = (int*)rr_take(base, &off, 64);
+  s->count = ctx->dcount;
+  return 0;
+}
 
-  cudaStream_t st = S_(ctx);
-  gb_prof_rec pr, ps;
-  gb_prof_begin(ctx, &pr, GB_K_SYGV);
-  const double m3 = (double)m * m * m;
 #define RR_STAGE(cls, flops, launch) \
   gb_prof_begin(ctx, &ps, cls);      \
   launch;                            \
   gb_prof_end(ctx, &ps, 8.0 * m * m, flops)
+
+// steps 1-2 (shared by both paths): L, C = inv(L) A inv(L)' symmetrised
+static void rr_reduce(gpu_Context* ctx, double* A, double* B, int ld, int m, int* info,
+                      rr_scratch& s, int jacobi32, double report_below)
+{
+  cudaStream_t st = S_(ctx);
+  gb_prof_rec ps;
+  const double m3 = (double)m * m * m;
+  const size_t mm = (size_t)m * m;
   const unsigned tb = (unsigned)((m + 7) / 8);  // 8 warps (columns) per CTA
-  RR_STAGE(GB_K_RR_CHOL, m3 / 3, (rr_chol64_kernel<<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info)));
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(0, A, ld, s.W64, m, m, s)));
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(1, s.W64, m, s.C64, m, m, s)));
-  rr_sym_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
+  RR_STAGE(GB_K_RR_CHOL, m3 / 3, (rr_chol64_kernel<<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info, report_below)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(0, A, ld, s.W64, m, m, m, s)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(1, s.W64, m, s.C64, m, m, m, s)));
+  if (jacobi32) rr_sym_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
   rr_sym_store_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
+  gb_count_launch(4 + jacobi32);
+}
+
+static void rr_tridiag_path(gpu_Context* ctx, double* A, int ld, int m, int nev, double* w,
+                            int* info, rr_scratch& s)
+{
+  cudaStream_t st = S_(ctx);
+  gb_prof_rec ps;
+  const double m3 = (double)m * m * m;
+  RR_STAGE(GB_K_RR_TRID, 4.0 * m3 / 3.0, (rr_tridiag_kernel<<<1, RR_TRD_THREADS, 0, st>>>(m, s)));
+  RR_STAGE(GB_K_RR_EIG, 0.0, (rr_bisect_kernel<<<nev, 32, 0, st>>>(m, s)));
+  RR_STAGE(GB_K_RR_EIG, 0.0, (rr_invit_kernel<<<nev, 32, 0, st>>>(m, s)));
+  // Cholesky-QR twice: Z <- Z inv(U), U'U = Z'Z
+  const dim3 gs((nev + 31) / 32, (nev + 31) / 32, 1), gz((m + 31) / 32, (nev + 31) / 32, 1);
+  for (int round = 0; round < 2; round++) {
+    rr_gemm_t zz = {s.X, m, 1, s.X, m, s.S, nev, nev, nev, m};
+    RR_STAGE(GB_K_RR_GEMM, 2.0 * m * nev * nev, (rr_gemm_kernel<<<gs, 256, 0, st>>>(zz, zz, s.status)));
+    RR_STAGE(GB_K_RR_EIG, 0.0, (rr_cholinv_kernel<<<1, 256, 0, st>>>(nev, s)));
+    rr_gemm_t zu = {s.X, m, 0, s.P, nev, s.Xn, m, m, nev, nev};
+    RR_STAGE(GB_K_RR_GEMM, 2.0 * m * nev * nev, (rr_gemm_kernel<<<gz, 256, 0, st>>>(zu, zu, s.status)));
+    double* t = s.X;
+    s.X = s.Xn;
+    s.Xn = t;
+  }
+  const unsigned tv = (unsigned)((nev + 7) / 8);
+  RR_STAGE(GB_K_RR_TRSM, 2.0 * m * m * nev, (rr_backtr_kernel<<<tv, 256, 0, st>>>(m, nev, s)));
+  RR_STAGE(GB_K_RR_TRSM, (double)m * m * nev,
+           (rr_trsm64_kernel<<<tv, 256, 0, st>>>(2, s.X, m, A, ld, m, nev, s)));
+  rr_finish_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(nev, s, w, info);
+  gb_count_launch(12);
+}
+
+static void rr_jacobi32_path(gpu_Context* ctx, double* A, int ld, int m, int nev, double* w,
+                             int* info, rr_scratch& s)
+{
+  cudaStream_t st = S_(ctx);
+  gb_prof_rec ps;
+  const double m3 = (double)m * m * m;
   // Jacobi: every CTA holds C (m*m) and `rows` rows of V
   const int nsplit = m <= 96 ? 1 : 4;
   const int rows = (m + nsplit - 1) / nsplit;
@@ -671,7 +1086,7 @@ extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, do
   cudaFuncSetAttribute(rr_jacobi32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_jac);
   RR_STAGE(GB_K_RR_JAC32, 0.0, (rr_jacobi32_kernel<<<nsplit, RR_THREADS, sm_jac, st>>>(m, rows, s)));
   rr_vsort_kernel<<<1, RR_THREADS, 0, st>>>(m, s);
-  int launches = 7;
+  int launches = 2;
   const size_t sm_ref = 2 * sizeof(double) * RR_CLUSTER_SMEM * rr_pad(RR_CLUSTER_SMEM);
   cudaFuncSetAttribute(rr_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_ref);
   const dim3 g1((m + 31) / 32, (m + 31) / 32, 1), g2((m + 31) / 32, (m + 31) / 32, 2);
@@ -692,12 +1107,33 @@ extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, do
     launches += 5;
   }
   // eigenvectors of the pencil: inv(L)' X into A; values into w
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(2, s.X, m, A, ld, m, s)));
-  rr_finish_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(m, s, w, info);
+  const unsigned tb = (unsigned)((m + 7) / 8);
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(2, s.X, m, A, ld, m, m, s)));
+  rr_finish_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(nev, s, w, info);
+  gb_count_launch(launches + 2);
+}
 #undef RR_STAGE
-  launches += 2;
-  gb_prof_end(ctx, &pr, 32.0 * m * m, 16.0 * m3);
-  gb_count_launch(launches);
+
+extern "C" int gb_sygv(gpu_Context* ctx, double* A, double* B, int ld, int m, int nev, double* w,
+                       int* info, double report_below)
+{
+  ctx->sygv_calls++;
+  const int forced = ctx->opt.sygv_fail_at > 0 && ctx->sygv_calls == ctx->opt.sygv_fail_at;
+  const int method = ctx->opt.rr_method;
+  if (nev < 1 || nev > m) nev = m;
+  if (forced || m < 2 || m > RR_MAX_M || method == 1 || (method == 2 && m > RR_MAX_SMEM_M))
+    return gb_sygv_fp64(ctx, A, B, ld, m, w, info, NULL, forced);
+  rr_scratch s;
+  if (rr_scratch_setup(ctx, m, &s)) return -1;
+  gb_prof_rec pr;
+  const double m3 = (double)m * m * m;
+  gb_prof_begin(ctx, &pr, GB_K_SYGV);
+  rr_reduce(ctx, A, B, ld, m, info, s, method == 2, report_below);
+  if (method == 2)
+    rr_jacobi32_path(ctx, A, ld, m, nev, w, info, s);
+  else
+    rr_tridiag_path(ctx, A, ld, m, nev, w, info, s);
+  gb_prof_end(ctx, &pr, 32.0 * m * m, 4.0 * m3);
   if (gb_cuda_check(ctx, (int)cudaGetLastError(), "rayleigh_ritz")) return -1;
   // FP64 Jacobi on the original pencil when the fast path did not finish
   return gb_sygv_fp64(ctx, A, B, ld, m, w, info, s.status, 0);

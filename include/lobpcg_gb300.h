@@ -40,8 +40,10 @@ typedef struct {
   int tensor_cores;         /* mixed: 1 = tcgen05 TF32 kernels, 0 = FP32 CUDA-core kernels */
   int potrf_fail_at;        /* tests: the Nth Cholesky reports INFO = 1 (0 = off) */
   int sygv_fail_at;         /* tests: the Nth Rayleigh-Ritz solve reports INFO = 1 (0 = off) */
-  int rr_fp64_only;         /* 1: Rayleigh-Ritz by the one-CTA FP64 Jacobi solver only (default 0:
-                               FP32 Jacobi + FP64 refinement, FP64 Jacobi as fallback) */
+  int rr_method;            /* Rayleigh-Ritz solver: 0 = FP64 Householder tridiagonalisation,
+                               bisection and inverse iteration (default); 1 = one-CTA FP64
+                               Jacobi; 2 = FP32 Jacobi + FP64 refinement (order <= 192).
+                               1 is also the fallback of 0 and 2. */
 } lobpcg_gpu_options;
 
 typedef struct {
@@ -57,6 +59,8 @@ typedef struct {
   int rr_jacobi32_sweeps;   /* FP32 Jacobi sweeps summed over those solves */
   int rr_max_cluster;       /* largest cluster of close Ritz values refined together */
   int rr_fallbacks;         /* solves that fell back to the one-CTA FP64 Jacobi */
+  int rr_graded;            /* of those: pencils too graded for the tridiagonal solver */
+  int explicit_undos;       /* mixed: FP32 steps undone after a residual jump */
 } lobpcg_gpu_stats;
 
 /* per-kernel-class timing, collected with CUDA events on the context's

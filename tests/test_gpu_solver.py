@@ -183,18 +183,19 @@ def test_verbosity_output_format(ctx, capfd):
 @pytest.mark.parametrize("name", ["lap20_k10_maxit1000", "st7vc_12_k6_jacobi", "gen27_8_k4",
                                   "all_paths_lap6"])
 def test_rayleigh_ritz_paths_agree(ctx, name):
-    """The default Rayleigh-Ritz solver (FP32 Jacobi + FP64 refinement) and
-    the one-CTA FP64 Jacobi solver give the same solve."""
+    """The three Rayleigh-Ritz solvers (FP64 tridiagonal, FP64 Jacobi, FP32
+    Jacobi + FP64 refinement) give the same solve."""
     case = C.build(name)
     g = load(name)
     out = []
-    for fp64_only in (0, 1):
-        ctx.set_options(precision=S.FP64, rr_fp64_only=fp64_only)
+    for method in (0, 1, 2):
+        ctx.set_options(precision=S.FP64, rr_method=method)
         try:
             r, _ = run_case(ctx, case)
         finally:
-            ctx.set_options(rr_fp64_only=0)
+            ctx.set_options(rr_method=0)
         parity.check(g, r.flag, r.iterations, r.lam)
         out.append(r)
     if out[0].flag == 0:
-        np.testing.assert_allclose(out[0].lam, out[1].lam, rtol=max(1e-10, 3 * _spread(g)))
+        for r in out[1:]:
+            np.testing.assert_allclose(out[0].lam, r.lam, rtol=max(1e-10, 3 * _spread(g)))
