@@ -44,6 +44,12 @@ CONFIGS = {
                label="3D 7-point Laplacian 20^3 CSR, k=10, no preconditioner, tol 1e-6, maxit 100"),
     "c2": dict(kind="csr", grid=(128, 128, 128), k=32, seed=1, tol=1e-8, maxit=300, jacobi=True,
                label="3D 7-point Laplacian 128^3 CSR (n=2097152), k=32, Jacobi, tol 1e-8, maxit 300"),
+    # matrix-free variable-coefficient stencil; a full solve to 1e-8 takes
+    # thousands of iterations, so this case is timed per iteration (maxit 20)
+    "c3": dict(kind="stencil7", grid=(256, 256, 256), k=64, seed=2, tol=1e-8, maxit=20,
+               jacobi=True,
+               label="matrix-free variable-coefficient 7-point stencil 256^3 (n=16777216), face "
+                     "coefficients exp(N(0,1)) seed 2, k=64, Jacobi, tol 1e-8, 20 iterations"),
 }
 
 
@@ -106,14 +112,90 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_problem(cfg):
+def fp64_peak_tflops(torch, n: int = 8192) -> float:
+    """FP64 GEMM throughput of this GPU (torch.matmul float64, best of 3,
+    CUDA events): the roof of the FP64 kernels, absent from the measured
+    peaks file."""
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        best = t if best is None else min(best, t)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best / 1e12
+
+
+# kernel classes whose arithmetic is FP64 in the FP64 path
+FP64_CLASSES = {"gram", "xc_update", "spmm_csr", "stencil7", "stencil5", "stencil27",
+                "diag_scale", "residual", "blas1"}
+
+
+def roofline_entry(name, v, hbm_peak, fp64_peak, traffic, fp64_arith=True, tf32_peak=None):
+    """Bound = whichever of HBM bytes / HBM peak and flops / compute peak is
+    longer (FP64 pipe for the FP64 classes, TF32 tensor rate for the tcgen05
+    classes); achieved = algorithmic bytes or flops per launch / event-timed
+    launch duration."""
+    sec = v["ms"] / 1e3
+    t_mem = v["bytes"] / (hbm_peak * 1e9)
+    t_fp = v["flops"] / (fp64_peak * 1e12) if (fp64_arith and name in FP64_CLASSES) else 0.0
+    t_tc = v["flops"] / (tf32_peak * 1e12) if (tf32_peak and name.startswith("tc_")) else 0.0
+    tr = traffic.get(name)
+    if t_fp > t_mem:
+        ach = v["flops"] / sec / 1e12
+        out = {"kernel": name, "bound": "fp64", "achieved": ach, "peak": fp64_peak,
+               "unit": "TFLOP/s", "frac": ach / fp64_peak,
+               "peak_kind": "measured in this run (torch.matmul float64 8192^3)"}
+    elif t_tc > t_mem:
+        ach = v["flops"] / sec / 1e12
+        out = {"kernel": name, "bound": "tensor", "achieved": ach, "peak": tf32_peak,
+               "unit": "TFLOP/s", "frac": ach / tf32_peak,
+               "peak_kind": "dense TF32 = half the measured bf16 burst rate"}
+    else:
+        ach = v["bytes"] / sec / 1e9
+        out = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+               "frac": ach / hbm_peak}
+    out.update({"traffic": tr["bytes_per_launch"] if tr else None,
+                "algorithmic_bytes_per_launch": v["bytes"] / v["launches"],
+                "algorithmic_flops_per_launch": v["flops"] / v["launches"],
+                "launches": v["launches"], "avg_launch_ms": v["ms"] / v["launches"]})
+    return out
+
+
+def load_traffic():
+    """DRAM bytes per launch from the committed ncu summary (profiles/)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def build_problem(cfg, grid=None):
+    """(n, operator description, host X0 or None, Jacobi diagonal or None).
+    X0 = 2*drand48()-1 from the config's seed; for the large stencil case it
+    is generated on the device (bit-identical) instead of on the host."""
     from blopex_gb300 import problems as P
-    nx, ny, nz = cfg["grid"]
+    nx, ny, nz = grid or cfg["grid"]
     n = nx * ny * nz
-    csr = P.laplacian3d_csr(nx, ny, nz)
-    x0 = P.drand48_block(n, cfg["k"], cfg["seed"])
-    tdiag = 1.0 / P.csr_diagonal(*csr) if cfg["jacobi"] else None
-    return n, csr, x0, tdiag
+    if cfg["kind"] == "csr":
+        op = ("csr", P.laplacian3d_csr(nx, ny, nz))
+        diag = P.csr_diagonal(*op[1])
+    else:
+        cx, cy, cz = P.stencil7_coefficients(nx, ny, nz, seed=cfg["seed"])
+        op = ("stencil7", (cx, cy, cz))
+        diag = P.stencil7_diagonal(cx, cy, cz)
+    x0 = P.drand48_block(n, cfg["k"], cfg["seed"]) if n * cfg["k"] <= (1 << 27) else None
+    tdiag = 1.0 / diag if cfg["jacobi"] else None
+    return n, op, x0, tdiag
 
 
 def cpu_baseline(cfg, budget_s: float = 25.0):
@@ -126,11 +208,10 @@ def cpu_baseline(cfg, budget_s: float = 25.0):
     nx, ny, nz = cfg["grid"]
     n_full = nx * ny * nz
     s = min(48, nx)
-    n = s * s * s
-    csr = P.laplacian3d_csr(s, s, s)
-    x0 = P.drand48_block(n, cfg["k"], cfg["seed"])
+    n, op, x0, tdiag = build_problem(cfg, (s, s, s))
+    csr = op[1] if op[0] == "csr" else P.stencil7_to_csr(*op[1])
     A = O.csr(*csr)
-    T = O.diag(1.0 / P.csr_diagonal(*csr)) if cfg["jacobi"] else O.NONE
+    T = O.diag(tdiag) if tdiag is not None else O.NONE
     t0 = time.perf_counter()
     O.solve(A, x0, T=T, atol=cfg["tol"], maxit=1, history=False)
     t1 = time.perf_counter()
@@ -189,12 +270,17 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--mode", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--maxit", type=int, default=0, help="override maxit (exploration only)")
+    ap.add_argument("--grid", type=int, default=0,
+                    help="override the grid edge (small cases for profiling only)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision arm")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
     if args.maxit:
         cfg["maxit"] = args.maxit
+    if args.grid:
+        cfg["grid"] = (args.grid,) * 3
+        cfg["label"] += f" [profiling case: grid {args.grid}^3]"
 
     if args.impl == "reference":
         run_reference(args, cfg)
@@ -216,14 +302,18 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    n, csr, x0, tdiag = build_problem(cfg)
+    n, op, x0, tdiag = build_problem(cfg)
     k = cfg["k"]
     ctx = S.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
-    A = S.CSRMatrix(ctx, *csr)
+    A = S.CSRMatrix(ctx, *op[1]) if op[0] == "csr" else S.Stencil7(ctx, *op[1])
     T = S.Diagonal(ctx, tdiag) if tdiag is not None else None
     X = S.MultiVector(ctx, n, k)
-    X0 = S.MultiVector.from_host(ctx, x0)
+    if x0 is not None:
+        X0 = S.MultiVector.from_host(ctx, x0)
+    else:
+        X0 = S.MultiVector(ctx, n, k)
+        X0.set_random(cfg["seed"])
 
     def solve(mode):
         ctx.set_options(precision=S.FP64 if mode == "fp64" else S.MIXED)
@@ -260,7 +350,11 @@ def main():
     res = results[-1]
 
     # e2e: X0 from pinned host memory, Ritz vectors back, every step
-    pinned_in = torch.from_numpy(np.asfortranarray(x0).ravel(order="F")).pin_memory()
+    if x0 is not None:
+        pinned_in = torch.from_numpy(np.asfortranarray(x0).ravel(order="F")).pin_memory()
+    else:
+        pinned_in = torch.empty(n * k, dtype=torch.float64).pin_memory()
+        X0.download_ptr(pinned_in.data_ptr(), n)
     pinned_out = torch.empty(n * k, dtype=torch.float64).pin_memory()
     ctx.set_options(precision=S.FP64 if args.mode == "fp64" else S.MIXED)
     e2e_times = []
@@ -279,32 +373,51 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e = float(t.item())
 
-    # the mixed-precision arm on the same problem (one solve, timed)
+    pk, pk_kind = peaks()
+    fp64_peak = fp64_peak_tflops(torch)
+    tf32_peak = pk["bf16_tflops"] / 2.0
+    traffic = load_traffic()
+
+    # the mixed-precision arm on the same problem (one solve, timed, with
+    # its own kernel breakdown)
     mixed = None
     if args.mode == "fp64" and not args.no_mixed:
+        ctx.profiling(True)
+        ctx.reset_kernel_times()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rm = solve("mixed")
         torch.cuda.synchronize()
         tm = time.perf_counter() - t0
-        mixed = {"seconds": tm, "flag": rm.flag, "iterations": rm.iterations,
-                 "iterations_fp32": rm.stats["iterations_fp32"],
-                 "iterations_fp64": rm.stats["iterations_fp64"],
+        kt_m = ctx.kernel_times()
+        ctx.profiling(False)
+        tot_m = sum(v["ms"] for v in kt_m.values()) or 1.0
+        st = rm.stats
+        mixed = {"seconds": tm, "seconds_per_iteration": tm / max(rm.iterations, 1),
+                 "flag": rm.flag, "iterations": rm.iterations,
+                 "iterations_fp32": st["iterations_fp32"],
+                 "iterations_compensated": st["iterations_compensated"],
+                 "iterations_fp64": st["iterations_fp64"],
+                 "explicit_undos": st["explicit_undos"],
                  "max_rel_lambda_diff_vs_fp64": float(np.max(np.abs(rm.lam - res.lam) /
                                                              np.abs(res.lam))),
-                 "final_max_residual": float(np.max(rm.res))}
-
-    pk, pk_kind = peaks()
+                 "final_max_residual": float(np.max(rm.res)),
+                 "kernels": {nm: {"share": v["ms"] / tot_m, "launches": v["launches"],
+                                  "avg_ms": v["ms"] / v["launches"]}
+                             for nm, v in sorted(kt_m.items(), key=lambda kv: -kv[1]["ms"])[:10]},
+                 "roofline": {nm: roofline_entry(nm, kt_m[nm], pk["hbm_gbs"], fp64_peak, traffic,
+                                                 fp64_arith=False, tf32_peak=tf32_peak)
+                              for nm in ("tc_gram", "stencil7", "spmm_csr", "xc_update")
+                              if nm in kt_m}}
     total_ms = sum(v["ms"] for v in ktimes.values()) or 1.0
     dom_name, dom = max(ktimes.items(), key=lambda kv: kv[1]["ms"])
-    achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
-    roofline = {"kernel": dom_name, "bound": "hbm", "achieved": achieved,
-                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                "peak_kind": pk_kind, "traffic": None,
-                "share_of_kernel_time": dom["ms"] / total_ms,
-                "launches": dom["launches"], "avg_launch_ms": dom["ms"] / dom["launches"],
-                "achieved_tflops": dom["flops"] / (dom["ms"] / 1e3) / 1e12}
-    spmm = ktimes.get("spmm_csr")
+    roofline = roofline_entry(dom_name, dom, pk["hbm_gbs"], fp64_peak, traffic)
+    if roofline["bound"] == "hbm":
+        roofline["peak_kind"] = pk_kind
+    roofline["share_of_kernel_time"] = dom["ms"] / total_ms
+    roofline["fp64_peak_tflops"] = fp64_peak
+    spmm_name = "spmm_csr" if op[0] == "csr" else "stencil7"
+    spmm = ktimes.get(spmm_name)
     kernels = {nm: {"share": v["ms"] / total_ms, "launches": v["launches"],
                     "avg_ms": v["ms"] / v["launches"],
                     "gbs": v["bytes"] / (v["ms"] / 1e3) / 1e9,
@@ -317,13 +430,12 @@ def main():
             "dtype": "f64" if args.mode == "fp64" else "f32+f64", "data": "synthetic",
             "config": config_block(cfg, args),
             "result": {"flag": res.flag, "iterations": res.iterations,
+                       "seconds_per_iteration": secs / max(res.iterations, 1),
                        "lambda_min": float(res.lam[0]), "lambda_max": float(res.lam[-1]),
                        "max_residual": float(np.max(res.res))},
             "roofline": roofline,
-            "spmm": None if spmm is None else {
-                "gbs": spmm["bytes"] / (spmm["ms"] / 1e3) / 1e9,
-                "frac_hbm": spmm["bytes"] / (spmm["ms"] / 1e3) / 1e9 / pk["hbm_gbs"],
-                "avg_launch_ms": spmm["ms"] / spmm["launches"]},
+            "spmm": None if spmm is None else roofline_entry(spmm_name, spmm, pk["hbm_gbs"],
+                                                             fp64_peak, traffic),
             "kernels": kernels,
             "mixed": mixed,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": n * k * 8,

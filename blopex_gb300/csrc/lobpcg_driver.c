@@ -707,8 +707,15 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         comp = 1;
         stall = 0;
       }
-      if (mx < 0.999 * best) {
-        best = mx;
+      /* progress: the mean log residual over all k columns (the largest
+         active residual plateaus for long stretches on clustered spectra
+         while the others converge); FP32 has reached its floor when that
+         mean sets no new minimum (by 0.1 %) for stall_limit iterations */
+      double lg = 0.0;
+      for (int i = 0; i < k; i++) lg += log(s->h_norm[i] + DBL_MIN);
+      lg /= k;
+      if (lg < best - 1e-3) {
+        best = lg;
         stall = 0;
       } else if (++stall >= ctl->stall_limit) {
         if (tc_ok && !comp) {

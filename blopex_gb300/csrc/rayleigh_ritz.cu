@@ -744,6 +744,96 @@ __global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_kernel(int m, rr_sc
   }
 }
 
+// The same reduction with the lower triangle packed in shared memory
+// (column c starts at c*m - c(c-1)/2), for m <= RR_TRD_SMEM_M: every pass is
+// a warp-parallel sweep with shuffle reductions, no global-memory latency
+// inside the m - 2 sequential steps.
+#define RR_TRD_SMEM_M 224
+__device__ __forceinline__ int rr_pk(int r, int c, int m) { return c * m - ((c * (c - 1)) >> 1) + (r - c); }
+
+__global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_smem_kernel(int m, rr_scratch s)
+{
+  extern __shared__ double Lp[];  // packed lower triangle, m(m+1)/2
+  __shared__ double v[RR_TRD_SMEM_M], p[RR_TRD_SMEM_M], p2[RR_TRD_SMEM_M];
+  __shared__ double red[RR_TRD_THREADS / 32];
+  __shared__ double sh_tau, sh_scale;
+  if (s.status[0]) return;
+  double* A = s.C64;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = nt >> 5;
+  for (int c = warp; c < m; c += nw)
+    for (int r = c + lane; r < m; r += 32) Lp[rr_pk(r, c, m)] = A[r + (size_t)c * m];
+  __syncthreads();
+  for (int j = 0; j + 2 < m; j++) {
+    const int n1 = m - j - 1, o = j + 1;  // trailing block rows/cols o .. m-1
+    const int cj = rr_pk(o, j, m);        // x = Lp[cj .. cj + n1)
+    double acc = 0.0;
+    for (int i = 1 + tid; i < n1; i += nt) acc += Lp[cj + i] * Lp[cj + i];
+    acc = rr_block_sum(acc, red);
+    if (tid == 0) {
+      const double alpha = Lp[cj];
+      double tau = 0.0, beta = alpha, scale = 0.0;
+      if (acc > 0.0) {
+        beta = -copysign(hypot(alpha, sqrt(acc)), alpha);
+        tau = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      s.d[j] = Lp[rr_pk(j, j, m)];
+      s.e[j] = beta;
+      s.tau[j] = tau;
+      sh_tau = tau;
+      sh_scale = scale;
+    }
+    __syncthreads();
+    const double tau = sh_tau, scale = sh_scale;
+    if (tau == 0.0) continue;  // uniform
+    for (int i = tid; i < n1; i += nt) {
+      const double vi = (i == 0) ? 1.0 : Lp[cj + i] * scale;
+      v[i] = vi;
+      if (i > 0) A[(o + i) + (size_t)j * m] = vi;  // reflector for the back-transformation
+    }
+    __syncthreads();
+    // p = A22 v: columns (r >= c) by even warps' share, rows (c < r) by all
+    for (int c = warp; c < n1; c += nw) {
+      const int base = rr_pk(o + c, o + c, m) - c;  // (r, c) at base + r
+      double t = 0.0;
+      for (int r = c + lane; r < n1; r += 32) t += Lp[base + r] * v[r];
+      t = rr_warp_sum(t);
+      if (lane == 0) p[c] = t;
+    }
+    for (int r = warp; r < n1; r += nw) {
+      double t = 0.0;
+      for (int c = lane; c < r; c += 32) t += Lp[rr_pk(o + r, o + c, m)] * v[c];
+      t = rr_warp_sum(t);
+      if (lane == 0) p2[r] = t;
+    }
+    __syncthreads();
+    acc = 0.0;
+    for (int i = tid; i < n1; i += nt) {
+      const double pi = tau * (p[i] + p2[i]);
+      p[i] = pi;
+      acc += pi * v[i];
+    }
+    const double K = 0.5 * tau * rr_block_sum(acc, red);  // (the sum's barriers order p)
+    for (int i = tid; i < n1; i += nt) p[i] -= K * v[i];  // p <- w
+    __syncthreads();
+    for (int c = warp; c < n1; c += nw) {
+      const int base = rr_pk(o + c, o + c, m) - c;
+      const double vc = v[c], wc = p[c];
+      for (int r = c + lane; r < n1; r += 32) Lp[base + r] -= v[r] * wc + p[r] * vc;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (m >= 2) {
+      s.d[m - 2] = Lp[rr_pk(m - 2, m - 2, m)];
+      s.e[m - 2] = Lp[rr_pk(m - 1, m - 2, m)];
+      s.tau[m - 2] = 0.0;
+    }
+    s.d[m - 1] = Lp[rr_pk(m - 1, m - 1, m)];
+  }
+}
+
 // number of eigenvalues of T below x (Sturm count of the LDL' pivots)
 __device__ __forceinline__ int rr_sturm(const double* d, const double* e2, int m, double x,
                                         double pivmin)
@@ -1050,7 +1140,14 @@ static void rr_tridiag_path(gpu_Context* ctx, double* A, int ld, int m, int nev,
   cudaStream_t st = S_(ctx);
   gb_prof_rec ps;
   const double m3 = (double)m * m * m;
-  RR_STAGE(GB_K_RR_TRID, 4.0 * m3 / 3.0, (rr_tridiag_kernel<<<1, RR_TRD_THREADS, 0, st>>>(m, s)));
+  if (m <= RR_TRD_SMEM_M) {
+    const int sm = (int)(sizeof(double) * (size_t)m * (m + 1) / 2);
+    cudaFuncSetAttribute(rr_tridiag_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    RR_STAGE(GB_K_RR_TRID, 4.0 * m3 / 3.0,
+             (rr_tridiag_smem_kernel<<<1, RR_TRD_THREADS, sm, st>>>(m, s)));
+  } else {
+    RR_STAGE(GB_K_RR_TRID, 4.0 * m3 / 3.0, (rr_tridiag_kernel<<<1, RR_TRD_THREADS, 0, st>>>(m, s)));
+  }
   RR_STAGE(GB_K_RR_EIG, 0.0, (rr_bisect_kernel<<<nev, 32, 0, st>>>(m, s)));
   RR_STAGE(GB_K_RR_EIG, 0.0, (rr_invit_kernel<<<nev, 32, 0, st>>>(m, s)));
   // Cholesky-QR twice: Z <- Z inv(U), U'U = Z'Z
