@@ -147,6 +147,7 @@ SIGNATURES = {
     "gpu_OperatorApply": (None, [c_void_p, c_void_p, c_void_p]),
     "gpu_ExplicitGram": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_int, c_void_p, c_void_p, c_int]),
+    "gpu_BlockUpdate": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int]),
     "gpu_GramNoAlloc": (c_int, [c_int, c_long, c_void_p, c_long, c_int, c_void_p, c_long, c_int,
                                 c_void_p, c_int, c_void_p]),
 }

@@ -126,6 +126,13 @@ int gb_tc_gram(gpu_Context* ctx, long n, const blk_cols* X, int k, const blk_col
                const blk_cols* P, int nP, const blk_cols* AX, const blk_cols* AR,
                const blk_cols* AP, int compensated, double* G, double* H, int ld);
 
+/* Y = X C (+ Z) on the tensor cores, compensated TF32 (tc_xc.cu): FP32
+   columns, h <= 128, w <= 64, C FP64 on the device (leading dimension ldc) */
+int gb_tc_xc(gpu_Context* ctx, long n, const blk_cols* X, int h, const double* C, int ldc,
+             const blk_cols* Y, int w, const blk_cols* Z);
+/* device error word of the tensor-core kernels (0 = none); clears it */
+int gb_device_error(gpu_Context* ctx, int* err);
+
 /* ---------------- small dense FP64 (dense.cu) ---------------- */
 /* in place: A(0:m,0:m) upper Cholesky factor U (A = U'U from the upper
    triangle), then A <- inv(U) with the strict lower part cleared; *info

@@ -831,10 +831,15 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         int off2 = cols_idx(srcs[q][0], NULL, nR, &a, 0);
         cols_idx(srcs[q][1], act, use_p, &a, off2);
         cols_idx(srcs[q][2], NULL, k, &y, 0);
-        if (gb_bymat(s->ctx, s->dt, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
         cols_idx(xs[q][0], NULL, k, &xa, 0);
         cols_idx(xs[q][1], NULL, k, &z, 0);
-        if (gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
+        if (tc_ok) {
+          if (gb_tc_xc(s->ctx, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
+          if (gb_tc_xc(s->ctx, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
+        } else {
+          if (gb_bymat(s->ctx, s->dt, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
+          if (gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
+        }
       }
       /* swap the double buffers */
       gpu_MultiVector* t;
@@ -860,6 +865,15 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     memcpy(prev_norm, s->h_norm, sizeof(double) * k);
     if (fetch_lambda(s)) return -2;
     int undo = nonfinite(s->h_lam, k);
+    if (tc_ok) {
+      int derr = 0;
+      if (gb_device_error(s->ctx, &derr)) return -2;
+      if (derr) {
+        /* a tensor-core kernel gave up waiting: its output is incomplete */
+        tc_ok = 0;
+        undo = 1;
+      }
+    }
     if (!undo) {
       if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
       /* A Ritz pair of the FP32 pencil that is not one of the operator

@@ -745,18 +745,38 @@ __global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_kernel(int m, rr_sc
 }
 
 // The same reduction with the lower triangle packed in shared memory
-// (column c starts at c*m - c(c-1)/2), for m <= RR_TRD_SMEM_M: every pass is
-// a warp-parallel sweep with shuffle reductions, no global-memory latency
-// inside the m - 2 sequential steps.
+// (column c starts at c*m - c(c-1)/2), for m <= RR_TRD_SMEM_M.  On this GPU a
+// warp-wide FP64 instruction occupies the FP64 pipe ~16 cycles whatever its
+// lane count, so the passes avoid shuffle-tree reductions: p = A22 v is one
+// thread per row (column part j <= i reads consecutive addresses across the
+// warp, row part j > i walks the thread's own column), the two scalar sums
+// are done by warp 0 alone.
 #define RR_TRD_SMEM_M 224
 __device__ __forceinline__ int rr_pk(int r, int c, int m) { return c * m - ((c * (c - 1)) >> 1) + (r - c); }
+
+// sum over threads of v, computed by warp 0 from per-thread values staged in
+// buf (blockDim.x entries); all threads return the sum
+__device__ double rr_sum_w0(double v, double* buf, double* out)
+{
+  const int tid = threadIdx.x;
+  buf[tid] = v;
+  __syncthreads();
+  if (tid < 32) {
+    double t = 0.0;
+    for (int i = tid; i < (int)blockDim.x; i += 32) t += buf[i];
+    t = rr_warp_sum(t);
+    if (tid == 0) *out = t;
+  }
+  __syncthreads();
+  return *out;
+}
 
 __global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_smem_kernel(int m, rr_scratch s)
 {
   extern __shared__ double Lp[];  // packed lower triangle, m(m+1)/2
-  __shared__ double v[RR_TRD_SMEM_M], p[RR_TRD_SMEM_M], p2[RR_TRD_SMEM_M];
-  __shared__ double red[RR_TRD_THREADS / 32];
-  __shared__ double sh_tau, sh_scale;
+  __shared__ double v[RR_TRD_SMEM_M], p[RR_TRD_SMEM_M];
+  __shared__ double buf[RR_TRD_THREADS];
+  __shared__ double sh_sum, sh_tau, sh_scale;
   if (s.status[0]) return;
   double* A = s.C64;
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -767,22 +787,24 @@ __global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_smem_kernel(int m, 
   for (int j = 0; j + 2 < m; j++) {
     const int n1 = m - j - 1, o = j + 1;  // trailing block rows/cols o .. m-1
     const int cj = rr_pk(o, j, m);        // x = Lp[cj .. cj + n1)
-    double acc = 0.0;
-    for (int i = 1 + tid; i < n1; i += nt) acc += Lp[cj + i] * Lp[cj + i];
-    acc = rr_block_sum(acc, red);
-    if (tid == 0) {
-      const double alpha = Lp[cj];
-      double tau = 0.0, beta = alpha, scale = 0.0;
-      if (acc > 0.0) {
-        beta = -copysign(hypot(alpha, sqrt(acc)), alpha);
-        tau = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
+    if (warp == 0) {
+      double acc = 0.0;
+      for (int i = 1 + lane; i < n1; i += 32) acc += Lp[cj + i] * Lp[cj + i];
+      acc = rr_warp_sum(acc);
+      if (lane == 0) {
+        const double alpha = Lp[cj];
+        double tau = 0.0, beta = alpha, scale = 0.0;
+        if (acc > 0.0) {
+          beta = -copysign(hypot(alpha, sqrt(acc)), alpha);
+          tau = (beta - alpha) / beta;
+          scale = 1.0 / (alpha - beta);
+        }
+        s.d[j] = Lp[rr_pk(j, j, m)];
+        s.e[j] = beta;
+        s.tau[j] = tau;
+        sh_tau = tau;
+        sh_scale = scale;
       }
-      s.d[j] = Lp[rr_pk(j, j, m)];
-      s.e[j] = beta;
-      s.tau[j] = tau;
-      sh_tau = tau;
-      sh_scale = scale;
     }
     __syncthreads();
     const double tau = sh_tau, scale = sh_scale;
@@ -793,30 +815,25 @@ __global__ void __launch_bounds__(RR_TRD_THREADS) rr_tridiag_smem_kernel(int m, 
       if (i > 0) A[(o + i) + (size_t)j * m] = vi;  // reflector for the back-transformation
     }
     __syncthreads();
-    // p = A22 v: columns (r >= c) by even warps' share, rows (c < r) by all
-    for (int c = warp; c < n1; c += nw) {
-      const int base = rr_pk(o + c, o + c, m) - c;  // (r, c) at base + r
-      double t = 0.0;
-      for (int r = c + lane; r < n1; r += 32) t += Lp[base + r] * v[r];
-      t = rr_warp_sum(t);
-      if (lane == 0) p[c] = t;
-    }
-    for (int r = warp; r < n1; r += nw) {
-      double t = 0.0;
-      for (int c = lane; c < r; c += 32) t += Lp[rr_pk(o + r, o + c, m)] * v[c];
-      t = rr_warp_sum(t);
-      if (lane == 0) p2[r] = t;
-    }
-    __syncthreads();
-    acc = 0.0;
+    // p_i = tau * (sum_{c <= i} A22(i, c) v_c + sum_{r > i} A22(r, i) v_r)
+    double pv = 0.0;
     for (int i = tid; i < n1; i += nt) {
-      const double pi = tau * (p[i] + p2[i]);
-      p[i] = pi;
-      acc += pi * v[i];
+      double t = 0.0;
+      int a = rr_pk(o + i, o, m);  // (i, c = 0)
+      for (int c = 0; c <= i; c++) {
+        t += Lp[a] * v[c];
+        a += m - (o + c) - 1;  // next column, same row
+      }
+      const int b = rr_pk(o + i, o + i, m);
+      for (int r = i + 1; r < n1; r++) t += Lp[b + (r - i)] * v[r];
+      t *= tau;
+      p[i] = t;
+      pv += t * v[i];
     }
-    const double K = 0.5 * tau * rr_block_sum(acc, red);  // (the sum's barriers order p)
-    for (int i = tid; i < n1; i += nt) p[i] -= K * v[i];  // p <- w
+    const double K = 0.5 * tau * rr_sum_w0(pv, buf, &sh_sum);  // (its barriers order p)
+    for (int i = tid; i < n1; i += nt) p[i] -= K * v[i];     // p <- w
     __syncthreads();
+    // A22 -= v w' + w v' (lower): warp per column
     for (int c = warp; c < n1; c += nw) {
       const int base = rr_pk(o + c, o + c, m) - c;
       const double vc = v[c], wc = p[c];

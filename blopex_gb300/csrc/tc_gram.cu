@@ -32,11 +32,11 @@
 #include <stdint.h>
 
 #include "internal.h"
+#include "tc_common.cuh"
 
 #define TCG_THREADS 256
 #define TCG_PRODUCERS 224
 #define TCG_MAX_ROWS 4096
-#define TCG_WAIT_LIMIT (1L << 24)
 
 struct tcg_params {
   blk_cols cols;  // slot s (X R P AX AR AP), column c at cols.col[s * KP + c]
@@ -46,95 +46,6 @@ struct tcg_params {
   float* partial;  // [cta][tmem column][128 lanes]
   int* err;
 };
-
-// ------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-// bounded wait for the phase with the given parity; false on timeout/abort
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
-{
-  const uint32_t addr = smem_u32(bar);
-  for (long i = 0; i < TCG_WAIT_LIMIT; i++) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (*abort_flag) return false;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes)
-{
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait()
-{
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async()
-{
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
-{
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
-  d |= (uint64_t)1 << 46;                    // descriptor version
-  d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
-  return d;
-}
-
-// instruction descriptor: D = F32, A = B = TF32, both K-major, M x N
-__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N)
-{
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate)
-{
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   smem_u32(bar))
-               : "memory");
-}
 
 // ------------------------------------------------------------ tile plans
 // One MMA of the plan: A rows start at smem row a_row (128 rows), B rows at

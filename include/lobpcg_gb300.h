@@ -172,6 +172,16 @@ int gpu_ExplicitGram(gpu_MultiVector* X, gpu_MultiVector* R, gpu_MultiVector* P,
                      gpu_MultiVector* AX, gpu_MultiVector* AR, gpu_MultiVector* AP, int mode,
                      double* G_host, double* H_host, int ldh);
 
+/* Y(active) = X(active) C (+ Z(active)) for a host h x w column-major C
+   (leading dimension ldc; h, w = active widths of X and Y); the operation of
+   mv_MultiVectorByMatrix / serial_Multi_VectorByMatrix
+   (blopex_serial_double/multivector/multi_vector.c:474-524) with the fused
+   accumulate of the solver's X update.  mode 0: CUDA-core kernel (FP64 or FP32
+   blocks); mode 1: tensor cores, compensated 3xTF32 (FP32 blocks, h <= 128,
+   w <= 64, 16-byte aligned columns).  Z may be NULL. */
+int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_MultiVector* Y,
+                    gpu_MultiVector* Z, int mode);
+
 /* ---------------------------------------------------------------- */
 /* Gram product without any allocation                               */
 /* ---------------------------------------------------------------- */
