@@ -148,6 +148,12 @@ SIGNATURES = {
     "gpu_ExplicitGram": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_int, c_void_p, c_void_p, c_int]),
     "gpu_BlockUpdate": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int]),
+    "gpu_EigenvectorAdjoint": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                       c_double, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "gpu_OperatorParameterCount": (c_long, [c_void_p]),
+    "gpu_OperatorGradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "gpu_MassGradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "gpu_GramNoAlloc": (c_int, [c_int, c_long, c_void_p, c_long, c_int, c_void_p, c_long, c_int,
                                 c_void_p, c_int, c_void_p]),
 }

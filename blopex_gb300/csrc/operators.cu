@@ -587,3 +587,198 @@ extern "C" int gpu_OperatorDiagonal(gpu_Operator* op, double* host_diag)
   }
   return gb_fail(ctx, "operator diagonal: unknown kind");
 }
+
+// ------------------------------------------------------------------------
+// Parameter gradients of sum_i w_i' A x_i (the adjoint contraction of the
+// eigenvalue / eigenvector derivatives): A is linear in its parameters, so
+// d/dtheta = sum_i w_i' (dA/dtheta) x_i, evaluated per parameter.  W holds
+// w_i = g_lambda_i x_i + mu_i (the output of gpu_EigenvectorAdjoint).
+// No counterpart in the reference (it has no derivatives).
+// ------------------------------------------------------------------------
+
+// sum_i (w_i[p] - w_i[q]) (x_i[p] - x_i[q]): a coupling of weight c between p
+// and q contributes c (e_p - e_q)(e_p - e_q)' to A; q < 0: c e_p e_p'
+__device__ __forceinline__ double grad_pair(const blk_cols& X, const blk_cols& W, int k, long p,
+                                            long q)
+{
+  double s = 0.0;
+  for (int i = 0; i < k; i++) {
+    const double* x = (const double*)X.col[i];
+    const double* w = (const double*)W.col[i];
+    if (q >= 0)
+      s += (w[p] - w[q]) * (x[p] - x[q]);
+    else
+      s += w[p] * x[p];
+  }
+  return s;
+}
+
+__global__ void grad_csr_kernel(long n, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                blk_cols X, blk_cols W, int k, double* __restrict__ g)
+{
+  const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  for (int e = rowptr[p]; e < rowptr[p + 1]; e++) {
+    const long q = colidx[e];
+    double s = 0.0;
+    for (int i = 0; i < k; i++) s += ((const double*)W.col[i])[p] * ((const double*)X.col[i])[q];
+    g[e] = s;
+  }
+}
+
+// faces of one direction of a grid stencil: face f = (a, b, c) with the face
+// coordinate `a` along the direction in [0, na]; cells (a-1) and a
+__global__ void grad_faces_kernel(int nx, int ny, int nz, int dir, blk_cols X, blk_cols W, int k,
+                                  double* __restrict__ g)
+{
+  const int ex = nx + (dir == 0), ey = ny + (dir == 1), ez = nz + (dir == 2);
+  const long nf = (long)ex * ey * ez;
+  const long f = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int i = (int)(f % ex), j = (int)((f / ex) % ey), l = (int)(f / ((long)ex * ey));
+  const int a = dir == 0 ? i : (dir == 1 ? j : l);
+  const int na = dir == 0 ? nx : (dir == 1 ? ny : nz);
+  const long stride = dir == 0 ? 1 : (dir == 1 ? (long)nx : (long)nx * ny);
+  const long cell_hi = (long)(dir == 0 ? (i < nx ? i : nx - 1) : i) +
+                       (long)nx * ((dir == 1 ? (j < ny ? j : ny - 1) : j) +
+                                   (long)ny * (dir == 2 ? (l < nz ? l : nz - 1) : l));
+  double s;
+  if (a == 0)
+    s = grad_pair(X, W, k, cell_hi, -1);
+  else if (a == na)
+    s = grad_pair(X, W, k, cell_hi, -1);  // cell_hi is the last cell here
+  else
+    s = grad_pair(X, W, k, cell_hi - stride, cell_hi);
+  g[f] = s;
+}
+
+__global__ void grad_st27_kernel(int nx, int ny, int nz, blk_cols X, blk_cols W, int k,
+                                 double* __restrict__ g)
+{
+  const long n = (long)nx * ny * nz;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= n * 13) return;
+  const long c = t / 13;
+  const int e = (int)(t % 13);
+  const int i = (int)(c % nx), j = (int)((c / nx) % ny), l = (int)(c / ((long)nx * ny));
+  const int di = c_st27_off[e][0], dj = c_st27_off[e][1], dk = c_st27_off[e][2];
+  const int i2 = i + di, j2 = j + dj, l2 = l + dk;
+  double s = 0.0;
+  if (i2 >= 0 && i2 < nx && j2 >= 0 && j2 < ny && l2 >= 0 && l2 < nz)
+    s = grad_pair(X, W, k, c, c + di + (long)nx * (dj + (long)ny * dk));
+  g[t] = s;  // cell-major, as the weights passed to gpu_Stencil27Create
+}
+
+__global__ void grad_diag_kernel(long n, blk_cols X, blk_cols W, int k, const double* lam,
+                                 const double* xg, double* __restrict__ g)
+{
+  const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  double s = 0.0;
+  for (int i = 0; i < k; i++) {
+    const double x = ((const double*)X.col[i])[p], w = ((const double*)W.col[i])[p];
+    s += lam ? -lam[i] * w * x - 0.5 * xg[i] * x * x : w * x;
+  }
+  g[p] = s;
+}
+
+static int grad_common(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* W, blk_cols* xc,
+                       blk_cols* wc)
+{
+  gpu_Context* ctx = op->ctx;
+  if (X->dtype != GPU_MV_FLOAT64 || W->dtype != GPU_MV_FLOAT64)
+    return gb_fail(ctx, "operator gradient: FP64 blocks expected");
+  if (X->size != op->n || W->size != op->n || X->num_active != W->num_active)
+    return gb_fail(ctx, "operator gradient: block sizes do not match the operator");
+  gb_mv_fill_cols(X, xc, 0);
+  gb_mv_fill_cols(W, wc, 0);
+  return 0;
+}
+
+extern "C" long gpu_OperatorParameterCount(gpu_Operator* op)
+{
+  switch (op->kind) {
+    case OPK_CSR: return op->nnz;
+    case OPK_ST7: return op->clen[0] + op->clen[1] + op->clen[2];
+    case OPK_ST5: return op->clen[0] + op->clen[1];
+    case OPK_ST27: return op->n * 13;
+    case OPK_DIAG: return op->n;
+  }
+  return -1;
+}
+
+extern "C" int gpu_OperatorGradient(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* W,
+                                    double* grad_host)
+{
+  gpu_Context* ctx = op->ctx;
+  blk_cols xc, wc;
+  if (grad_common(op, X, W, &xc, &wc)) return -1;
+  const int k = X->num_active;
+  const long np = gpu_OperatorParameterCount(op);
+  double* g = (double*)gb_device_alloc(ctx, sizeof(double) * (size_t)(np > 0 ? np : 1));
+  if (!g) return -1;
+  const long n = op->n;
+  int launches = 1;
+  switch (op->kind) {
+    case OPK_CSR:
+      grad_csr_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx, xc,
+                                                                        wc, k, g);
+      break;
+    case OPK_ST7:
+    case OPK_ST5: {
+      const int dirs = op->kind == OPK_ST7 ? 3 : 2;
+      long off = 0;
+      for (int d = 0; d < dirs; d++) {
+        grad_faces_kernel<<<(unsigned)((op->clen[d] + 255) / 256), 256, 0, S(ctx)>>>(
+            op->nx, op->ny, op->nz, d, xc, wc, k, g + off);
+        off += op->clen[d];
+      }
+      launches = dirs;
+      break;
+    }
+    case OPK_ST27:
+      grad_st27_kernel<<<(unsigned)((n * 13 + 255) / 256), 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz,
+                                                                             xc, wc, k, g);
+      break;
+    case OPK_DIAG:
+      grad_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S(ctx)>>>(n, xc, wc, k, NULL, NULL, g);
+      break;
+  }
+  gb_count_launch(launches);
+  int rc = gb_cuda_check(ctx, (int)cudaGetLastError(), "operator gradient");
+  if (!rc) rc = gb_memcpy_d2h(ctx, grad_host, g, sizeof(double) * (size_t)np);
+  gb_sync(ctx);
+  gb_device_free(g);
+  return rc;
+}
+
+extern "C" int gpu_MassGradient(gpu_Operator* B, gpu_MultiVector* X, gpu_MultiVector* W,
+                                const double* lambda, const double* xg, double* grad_host)
+{
+  gpu_Context* ctx = B->ctx;
+  if (B->kind != OPK_DIAG) return gb_fail(ctx, "mass gradient: B must be a diagonal operator");
+  blk_cols xc, wc;
+  if (grad_common(B, X, W, &xc, &wc)) return -1;
+  const int k = X->num_active;
+  const long n = B->n;
+  double* g = (double*)gb_device_alloc(ctx, sizeof(double) * ((size_t)n + 2 * (size_t)k));
+  if (!g) return -1;
+  double* lam = g + n;
+  double* xgd = lam + k;
+  int rc = gb_memcpy_h2d(ctx, lam, lambda, sizeof(double) * k);
+  if (!rc) {
+    if (xg)
+      rc = gb_memcpy_h2d(ctx, xgd, xg, sizeof(double) * k);
+    else
+      rc = cudaMemsetAsync(xgd, 0, sizeof(double) * k, S(ctx)) == cudaSuccess ? 0 : -1;
+  }
+  if (!rc) {
+    grad_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S(ctx)>>>(n, xc, wc, k, lam, xgd, g);
+    gb_count_launch(1);
+    rc = gb_cuda_check(ctx, (int)cudaGetLastError(), "mass gradient");
+  }
+  if (!rc) rc = gb_memcpy_d2h(ctx, grad_host, g, sizeof(double) * (size_t)n);
+  gb_sync(ctx);
+  gb_device_free(g);
+  return rc;
+}

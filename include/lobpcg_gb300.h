@@ -183,6 +183,50 @@ int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_Multi
                     gpu_MultiVector* Z, int mode);
 
 /* ---------------------------------------------------------------- */
+/* Derivatives of the computed eigenpairs (no counterpart in the      */
+/* reference)                                                          */
+/* ---------------------------------------------------------------- */
+
+/* Reverse mode for A x_i = lambda_i B x_i, X'BX = I (X: the n x k Ritz
+   vectors returned by lobpcg_solve_double, FP64).  Given G = dL/dX (n x k
+   FP64 block, or NULL) and glam = dL/dlambda (host k doubles, or NULL),
+   writes W (n x k FP64): w_i = glam_i x_i + mu_i with
+   mu_i = sum_{j != i} x_j (x_j'g_i) / (lambda_i - lambda_j) over the whole
+   spectrum: the part inside span(X) explicitly (pairs closer than
+   1e-12 max|lambda| are skipped), the rest by preconditioned conjugate
+   gradients on (A - lambda_i B) restricted to the B-orthogonal complement of
+   span(X), all columns in lockstep, until |r_i| <= tol |b_i| or maxit steps.
+   A, B, T are operator callbacks as in lobpcg_solve_double (B, T may be NULL;
+   T approximates the inverse of A).  xg (host k, may be NULL) receives
+   g_i'x_i for gpu_MassGradient.  Returns 0 or -1 (message:
+   gpu_ContextLastError); *iterations and *max_rel_residual report the solve. */
+int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, gpu_MultiVector* G,
+                           const double* glam, void* Adata, void (*A)(void*, void*, void*),
+                           void* Bdata, void (*B)(void*, void*, void*), void* Tdata,
+                           void (*T)(void*, void*, void*), double tol, int maxit,
+                           gpu_MultiVector* W, double* xg, int* iterations,
+                           double* max_rel_residual);
+
+/* Number of parameters of an operator: CSR nnz values; 7-point faces
+   (cx | cy | cz concatenated, the layouts of gpu_Stencil7Create); 5-point
+   faces (cx | cy); 27-point edge weights (cell-major n x 13, as passed to
+   gpu_Stencil27Create); diagonal n. */
+long gpu_OperatorParameterCount(gpu_Operator* op);
+
+/* grad (host, gpu_OperatorParameterCount doubles) = sum_i w_i' (dA/dtheta)
+   x_i for every parameter theta of A: with W from gpu_EigenvectorAdjoint this
+   is dL/dtheta through the eigenpairs (dlambda_i/dA = x_i x_i' on the CSR
+   pattern; a coupling c between cells p, q gives (w_p - w_q)(x_p - x_q),
+   a boundary face w_p x_p).  The shift is not a parameter. */
+int gpu_OperatorGradient(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* W,
+                         double* grad);
+
+/* grad (host, n) = dL/d(diagonal of B) for B = gpu_DiagonalCreate:
+   -sum_i lambda_i w_i o x_i - (1/2) sum_i xg_i x_i o x_i (xg may be NULL). */
+int gpu_MassGradient(gpu_Operator* B, gpu_MultiVector* X, gpu_MultiVector* W,
+                     const double* lambda, const double* xg, double* grad);
+
+/* ---------------------------------------------------------------- */
 /* Gram product without any allocation                               */
 /* ---------------------------------------------------------------- */
 
