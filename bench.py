@@ -46,6 +46,12 @@ CONFIGS = {
                label="3D 7-point Laplacian 128^3 CSR (n=2097152), k=32, Jacobi, tol 1e-8, maxit 300"),
     # matrix-free variable-coefficient stencil; a full solve to 1e-8 takes
     # thousands of iterations, so this case is timed per iteration (maxit 20)
+    # differentiation: forward solve + reverse-mode gradient in theta
+    "c4": dict(kind="adjoint5", grid=(512, 512), k=8, seed=3, tol=1e-8, maxit=3000,
+               jacobi=True, adjoint_tol=1e-8, inner_cg=20,
+               label="2D 5-point diffusion 512^2, c = exp(theta), theta GRF (length 0.1, seed 3), "
+                     "k=8, loss = sum(lambda) + (x_1'v)^2, d loss / d theta; FP64, tol 1e-8, "
+                     "preconditioner 20 Jacobi-CG steps on A"),
     "c3": dict(kind="stencil7", grid=(256, 256, 256), k=64, seed=2, tol=1e-8, maxit=20,
                jacobi=True,
                label="matrix-free variable-coefficient 7-point stencil 256^3 (n=16777216), face "
@@ -228,6 +234,112 @@ def cpu_baseline(cfg, budget_s: float = 25.0):
             "per_iteration_s_full_n": per_it * scale}
 
 
+def run_adjoint(args, cfg):
+    """--config c4: forward LOBPCG solve and reverse-mode gradient of the
+    loss through the adjoint module.  value = forward + backward ms per step
+    (device-resident coefficients and blocks, CUDA events on the solver
+    stream); e2e = the torch.autograd path from a host theta to host
+    d loss / d theta."""
+    import torch
+    from blopex_gb300 import adjoint as AD
+    from blopex_gb300 import problems as P
+    from blopex_gb300 import solver as S
+    nx, ny = cfg["grid"]
+    n, k = nx * ny, cfg["k"]
+    theta = 0.5 * P.gaussian_random_field(nx, ny, 0.1, cfg["seed"])
+    cx, cy = P.stencil5_from_cells(np.exp(theta))
+    v = np.random.default_rng(cfg["seed"]).standard_normal(n)
+    v /= np.linalg.norm(v)
+    ctx = S.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    A = S.Stencil5(ctx, cx, cy)
+    J = S.Diagonal(ctx, 1.0 / A.diagonal())
+    T = S.PCGPreconditioner(ctx, A, J, cfg["inner_cg"])
+    X = S.MultiVector(ctx, n, k)
+    ctx.set_options(precision=S.FP64)
+    glam = np.ones(k)
+
+    def forward():
+        X.set_random(1)
+        return S.lobpcg_solve_double(X, A, T=T, atol=cfg["tol"], rtol=1e-50, maxit=cfg["maxit"],
+                                     history=False)
+
+    def backward(r):
+        x1 = X.to_host()[:, 0]
+        G = np.zeros((n, k), order="F")
+        G[:, 0] = 2.0 * (x1 @ v) * v
+        adj = AD.eigenvector_adjoint(X, r.lam, A, G=G, glam=glam, T=T, tol=cfg["adjoint_tol"],
+                                     maxit=20000)
+        return adj, AD.operator_gradient(A, X, adj.W)
+
+    def timed(f, *a):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        out = f(*a)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        backward(forward())
+    ctx.profiling(True)
+    ctx.reset_kernel_times()
+    sampler = ClockSampler(0)
+    sampler.start()
+    launches0 = ctx.lib.gpu_KernelLaunchCount()
+    fwd, bwd, its, aits, res = [], [], 0, 0, 0.0
+    for _ in range(args.steps):
+        r, tf = timed(forward)
+        (adj, g), tb = timed(backward, r)
+        fwd.append(tf)
+        bwd.append(tb)
+        its, aits, res = r.iterations, adj.iterations, adj.max_rel_residual
+    launches = ctx.lib.gpu_KernelLaunchCount() - launches0
+    clocks = sampler.stop()
+    kt = ctx.kernel_times()
+    ctx.profiling(False)
+    tf, tb = statistics.median(fwd), statistics.median(bwd)
+
+    # e2e: host theta -> torch autograd -> host gradient, every step
+    opts = AD.SolveOptions(k=k, atol=cfg["tol"], maxit=cfg["maxit"], adjoint_tol=cfg["adjoint_tol"],
+                           adjoint_maxit=20000, inner_cg=cfg["inner_cg"])
+    vt = torch.from_numpy(v)
+    e2e = []
+    for _ in range(max(1, args.steps)):
+        th = torch.from_numpy(theta).requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c = torch.exp(th)
+        fx, fy = AD.stencil5_faces_torch(c)
+        lam, Xh = AD.Stencil5Eigs.apply(fx, fy, ctx, opts)
+        loss = lam.sum() + (Xh[:, 0] @ vt) ** 2
+        (gt,) = torch.autograd.grad(loss, th)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    pk, _ = peaks()
+    total = sum(v_["ms"] for v_ in kt.values()) or 1.0
+    line = {"metric": "fwd+bwd ms (forward solve + reverse-mode gradient)", "value": tf + tb,
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tf + tb, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": cfg["label"], "n": n, "k": k, "tol": cfg["tol"],
+                       "adjoint_tol": cfg["adjoint_tol"], "parallelism": "replicas",
+                       "l2": "inputs smaller than L2 (n*k*8 = 16.8 MB)"},
+            "forward_ms": tf, "backward_ms": tb, "fwd_plus_bwd_over_fwd": (tf + tb) / tf,
+            "lobpcg_iterations": its, "adjoint_cg_iterations": aits,
+            "adjoint_max_rel_residual": res,
+            "kernels": {nm: {"share": x["ms"] / total, "launches": x["launches"],
+                             "avg_ms": x["ms"] / x["launches"]}
+                        for nm, x in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])[:8]},
+            "e2e": {"value": statistics.median(e2e), "unit": "ms",
+                    "h2d_bytes_per_step": 8 * (cx.size + cy.size),
+                    "d2h_bytes_per_step": 8 * (n * k + k + cx.size + cy.size)},
+            "gpu_launches": int(launches), "clocks": clocks,
+            "roofline": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, cfg):
     """--impl reference: the CPU implementation of the path timed alone."""
     rank = int(os.environ.get("RANK", "0"))
@@ -283,7 +395,14 @@ def main():
         cfg["label"] += f" [profiling case: grid {args.grid}^3]"
 
     if args.impl == "reference":
+        if cfg["kind"] == "adjoint5":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no "
+                              "derivatives (no adjoint or gradient of its eigenpairs)"}), flush=True)
+            return
         run_reference(args, cfg)
+        return
+    if cfg["kind"] == "adjoint5":
+        run_adjoint(args, cfg)
         return
 
     import torch
@@ -382,6 +501,10 @@ def main():
     # its own kernel breakdown)
     mixed = None
     if args.mode == "fp64" and not args.no_mixed:
+        # warm-up of the mixed path (first launches, workspace growth)
+        ctx.set_options(precision=S.MIXED)
+        X.copy_from(X0)
+        S.lobpcg_solve_double(X, A, T=T, atol=cfg["tol"], rtol=1e-50, maxit=3, history=False)
         ctx.profiling(True)
         ctx.reset_kernel_times()
         torch.cuda.synchronize()

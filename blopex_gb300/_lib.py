@@ -144,6 +144,7 @@ SIGNATURES = {
     "gpu_DiagonalCreate": (c_void_p, [c_void_p, c_long, c_void_p]),
     "gpu_OperatorDiagonal": (c_int, [c_void_p, c_void_p]),
     "gpu_OperatorDestroy": (None, [c_void_p]),
+    "gpu_PCGPreconditionerCreate": (c_void_p, [c_void_p, c_void_p, c_void_p, c_int]),
     "gpu_OperatorApply": (None, [c_void_p, c_void_p, c_void_p]),
     "gpu_ExplicitGram": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_int, c_void_p, c_void_p, c_int]),

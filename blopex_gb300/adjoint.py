@@ -98,6 +98,14 @@ class SolveOptions:
     precision: int = S.FP64
     adjoint_tol: float = 1e-10
     adjoint_maxit: int = 5000
+    inner_cg: int = 0  # > 0: precondition with that many CG steps on A (else Jacobi)
+
+
+def _preconditioner(ctx: S.Context, A: S.Operator, opts: SolveOptions) -> S.Operator:
+    J = S.Diagonal(ctx, 1.0 / A.diagonal())
+    if opts.inner_cg > 0:
+        return S.PCGPreconditioner(ctx, A, J, opts.inner_cg)
+    return J
 
 
 def _solve(ctx: S.Context, A: S.Operator, B: Optional[S.Operator], T: Optional[S.Operator],
@@ -141,7 +149,7 @@ if torch is not None:
             cxn = cx.detach().cpu().numpy().astype(np.float64)
             cyn = cy.detach().cpu().numpy().astype(np.float64)
             A = S.Stencil5(ctx, cxn, cyn)
-            T = S.Diagonal(ctx, 1.0 / A.diagonal())
+            T = _preconditioner(ctx, A, opts)
             X, lam = _solve(ctx, A, None, T, opts)
             fctx.state = (ctx, A, T, X, lam, opts, cxn.shape, cyn.shape)
             return torch.from_numpy(lam), torch.from_numpy(X.to_host())
@@ -169,7 +177,7 @@ if torch is not None:
             bn = np.ascontiguousarray(b.detach().cpu().numpy(), dtype=np.float64)
             A = S.Stencil27(ctx, nx, ny, nz, wn, shift)
             B = S.Diagonal(ctx, bn)
-            T = S.Diagonal(ctx, 1.0 / A.diagonal())
+            T = _preconditioner(ctx, A, opts)
             X, lam = _solve(ctx, A, B, T, opts)
             fctx.state = (ctx, A, B, T, X, lam, opts, wn.shape)
             return torch.from_numpy(lam), torch.from_numpy(X.to_host())

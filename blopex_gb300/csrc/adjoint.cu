@@ -16,8 +16,11 @@
 // preconditioned conjugate gradients on the projected operator
 // P_L (A - lambda_i B) P_R (P_L = I - B X X', P_R = I - X X'B), all k columns
 // in lockstep (one block application of A and B per step, the projections as
-// k x k Gram products and block updates).  The eigenpairs are never stored
-// along the iteration history: the backward pass needs only the final X.
+// k x k Gram products and block updates).  The Polak-Ribiere form of beta
+// (r_new'(z_new - z_old) / r_old'z_old, restarted when negative) keeps the
+// iteration convergent when the preconditioner is itself an iteration (an
+// inner CG on A).  The eigenpairs are never stored along the iteration
+// history: the backward pass needs only the final X.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -45,6 +48,12 @@ __global__ void adj_inspace_kernel(int k, const double* __restrict__ Sg, const d
     v = fabs(d) > tol_deg ? Sg[j + (size_t)i * k] / d : 0.0;
   }
   M[j + (size_t)i * k] = v;
+}
+
+__global__ void adj_sub_kernel(int k, const double* a, const double* b, double* out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] = a[i] - b[i];
 }
 
 __global__ void adj_neg_kernel(int m, double* A)
@@ -106,7 +115,7 @@ struct adj_state {
   long n;
   int k;
   gpu_MultiVector *X, *BX, *G, *W;
-  gpu_MultiVector *mu, *r, *z, *p, *q, *t;
+  gpu_MultiVector *mu, *r, *z, *p, *q, *t, *zo;
   double *Sg, *M, *lam, *glam, *num, *den, *alpha, *rho, *rho2, *bn2;
 };
 
@@ -211,7 +220,7 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
   a.rho = a.alpha + k;
   a.rho2 = a.rho + k;
   a.bn2 = a.rho2 + k;
-  gpu_MultiVector* blocks[6] = {NULL, NULL, NULL, NULL, NULL, NULL};
+  gpu_MultiVector* blocks[7] = {NULL, NULL, NULL, NULL, NULL, NULL, NULL};
   int rc = 0, it = 0;
   double worst = 0.0;
   double* host = (double*)malloc(sizeof(double) * 2 * k);
@@ -223,7 +232,7 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
     else
       rc = cudaMemsetAsync(a.glam, 0, sizeof(double) * k, S(ctx)) == cudaSuccess ? 0 : -1;
   }
-  for (int b = 0; b < 6 && !rc; b++) {
+  for (int b = 0; b < 7 && !rc; b++) {
     blocks[b] = gb_mv_create_like(X, GPU_MV_FLOAT64);
     if (!blocks[b]) rc = -1;
   }
@@ -234,8 +243,9 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
     a.p = blocks[3];
     a.q = blocks[4];
     a.t = blocks[5];
-    gpu_MultiVector* all[6] = {a.mu, a.r, a.z, a.p, a.q, a.t};
-    for (int b = 0; b < 6; b++) gb_mv_set_mask_host(all[b], NULL);
+    a.zo = blocks[6];
+    gpu_MultiVector* all[7] = {a.mu, a.r, a.z, a.p, a.q, a.t, a.zo};
+    for (int b = 0; b < 7; b++) gb_mv_set_mask_host(all[b], NULL);
   }
   // B X (X itself when B is the identity)
   gpu_MultiVector* BXb = NULL;
@@ -245,7 +255,7 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
   }
   a.BX = BXb ? BXb : X;
 
-  blk_cols cx, cbx, cg, cw, cmu, cr, cz, cp, cq, ct;
+  blk_cols cx, cbx, cg, cw, cmu, cr, cz, cp, cq, ct, czo;
   if (!rc) {
     cols_of(X, &cx);
     cols_of(a.BX, &cbx);
@@ -256,6 +266,7 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
     cols_of(a.p, &cp);
     cols_of(a.q, &cq);
     cols_of(a.t, &ct);
+    cols_of(a.zo, &czo);
     if (G) cols_of(G, &cg);
   }
   const dim3 cgrid(row_blocks(ctx, a.n, k), k);
@@ -332,11 +343,15 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
         if (rel > worst) worst = rel;
       }
       if (worst <= tol2) break;
-      if (precond(&a, T, Tdata) || dots(&a, a.r, a.z, a.rho2)) {
+      // z_old = z; z = P_R T r; rho2 = r'z - r'z_old (Polak-Ribiere)
+      if (gb_axpby(ctx, GPU_MV_FLOAT64, a.n, 1.0, &cz, 0.0, &czo, k) || precond(&a, T, Tdata) ||
+          dots(&a, a.r, a.z, a.rho2) || dots(&a, a.r, a.zo, a.num)) {
         rc = -1;
         break;
       }
-      adj_ratio_kernel<<<1, 256, 0, S(ctx)>>>(k, a.rho2, a.rho, a.alpha);  // beta
+      adj_sub_kernel<<<1, 256, 0, S(ctx)>>>(k, a.rho2, a.num, a.den);  // den <- r'z - r'z_old
+      gb_count_launch(1);
+      adj_ratio_kernel<<<1, 256, 0, S(ctx)>>>(k, a.den, a.rho, a.alpha);  // beta
       adj_xpby_cols_kernel<<<cgrid, 256, 0, S(ctx)>>>(a.n, cz, cp, a.alpha);
       gb_count_launch(2);
       double* tswap = a.rho;
@@ -351,7 +366,7 @@ extern "C" int gpu_EigenvectorAdjoint(gpu_MultiVector* X, const double* lambda, 
   gb_sync(ctx);
   if (iterations) *iterations = G ? it : 0;
   if (max_rel_residual) *max_rel_residual = sqrt(worst);
-  for (int b = 0; b < 6; b++) gpu_MultiVectorDestroy(blocks[b]);
+  for (int b = 0; b < 7; b++) gpu_MultiVectorDestroy(blocks[b]);
   gpu_MultiVectorDestroy(BXb);
   gb_device_free(small);
   free(host);

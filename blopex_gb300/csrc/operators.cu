@@ -16,7 +16,7 @@
 
 #include "internal.h"
 
-enum { OPK_CSR = 1, OPK_ST7 = 2, OPK_ST5 = 3, OPK_ST27 = 4, OPK_DIAG = 5 };
+enum { OPK_CSR = 1, OPK_ST7 = 2, OPK_ST5 = 3, OPK_ST27 = 4, OPK_DIAG = 5, OPK_PCG = 6 };
 
 struct gpu_Operator {
   int kind;
@@ -36,6 +36,13 @@ struct gpu_Operator {
   float* w32;
   double* d;      // DIAG
   float* d32;
+  // PCG: `iters` steps of conjugate gradients on `inner` (preconditioned by
+  // `prec`, may be NULL) from a zero start; work blocks cached per shape
+  gpu_Operator* inner;
+  gpu_Operator* prec;
+  int iters;
+  gpu_MultiVector* work[4];  // r, z, p, q
+  double* coef;              // 4 x BLK_MAXCOLS device doubles
 };
 
 static inline cudaStream_t S(gpu_Context* ctx) { return (cudaStream_t)ctx->stream; }
@@ -255,6 +262,8 @@ extern "C" void gpu_OperatorDestroy(gpu_Operator* op)
   gb_device_free(op->w32);
   gb_device_free(op->d);
   gb_device_free(op->d32);
+  for (int b = 0; b < 4; b++) gpu_MultiVectorDestroy(op->work[b]);
+  gb_device_free(op->coef);
   free(op);
 }
 
@@ -397,8 +406,11 @@ static int ensure_f32(gpu_Operator* op)
   return 0;
 }
 
+static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
+
 extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
 {
+  if (op->kind == OPK_PCG) return pcg_apply(op, X, Y);
   gpu_Context* ctx = op->ctx;
   if (X->size != op->n || Y->size != op->n)
     return gb_fail(ctx, "operator of size %ld applied to blocks of %ld / %ld rows", op->n,
@@ -781,4 +793,140 @@ extern "C" int gpu_MassGradient(gpu_Operator* B, gpu_MultiVector* X, gpu_MultiVe
   gb_sync(ctx);
   gb_device_free(g);
   return rc;
+}
+
+// ------------------------------------------------------------------------
+// Inner conjugate-gradient preconditioner T ~ inv(A): Y = `iters` steps of
+// (preconditioned) CG on A Y = X from Y = 0, every column an independent
+// recurrence, all columns in lockstep (one block application of A per
+// step).  The preconditioner of HYPRE's LOBPCG driver with -pcgitr
+// (blopex_hypre/krylov/HYPRE_lobpcg.c:317-320, precondUsageMode): a fixed
+// number of CG steps, so T is only approximately linear, which LOBPCG
+// tolerates.  Works in the dtype of the blocks (FP32 in the FP32 phase).
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void pcg_cols_kernel(long n, int mode, blk_cols A, blk_cols B, blk_cols C, blk_cols D,
+                                const double* __restrict__ a)
+{
+  // mode 0: C_i = a_i A_i (first step: Y = alpha P), D_i -= a_i B_i
+  // mode 1: C_i += a_i A_i,  D_i -= a_i B_i
+  // mode 2: C_i = A_i + a_i C_i  (P = Z + beta P)
+  const int i = blockIdx.y;
+  const T ai = (T)a[i];
+  const T* x = (const T*)A.col[i];
+  const T* y = (const T*)B.col[i];
+  T* c = (T*)C.col[i];
+  T* d = (T*)D.col[i];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    if (mode == 2) {
+      c[r] = x[r] + ai * c[r];
+    } else {
+      c[r] = (mode == 0 ? T(0) : c[r]) + ai * x[r];
+      d[r] -= ai * y[r];
+    }
+  }
+}
+
+__global__ void pcg_ratio_kernel(int k, const double* num, const double* den, double* out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] = (den[i] != 0.0 && num[i] != 0.0) ? num[i] / den[i] : 0.0;
+}
+
+extern "C" gpu_Operator* gpu_PCGPreconditionerCreate(gpu_Context* ctx, gpu_Operator* A,
+                                                     gpu_Operator* M, int iterations)
+{
+  if (!A || iterations < 1 || (M && M->n != A->n)) {
+    gb_fail(ctx, "PCG preconditioner: bad arguments");
+    return NULL;
+  }
+  gpu_Operator* op = op_new(ctx, OPK_PCG, A->n);
+  op->inner = A;
+  op->prec = M;
+  op->iters = iterations;
+  op->coef = (double*)gb_device_alloc(ctx, sizeof(double) * 4 * BLK_MAXCOLS);
+  if (!op->coef) {
+    gpu_OperatorDestroy(op);
+    return NULL;
+  }
+  return op;
+}
+
+static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
+{
+  gpu_Context* ctx = op->ctx;
+  const int w = X->num_active;
+  if (X->size != op->n || Y->size != op->n || Y->num_active != w || X->dtype != Y->dtype)
+    return gb_fail(ctx, "PCG preconditioner: block shapes");
+  if (w == 0) return 0;
+  // work blocks of (at least) this width and dtype
+  gpu_MultiVector** wk = op->work;
+  if (!wk[0] || wk[0]->dtype != X->dtype || wk[0]->num_vectors < w) {
+    for (int b = 0; b < 4; b++) {
+      gpu_MultiVectorDestroy(wk[b]);
+      wk[b] = gpu_MultiVectorCreate(ctx, op->n, w, X->dtype);
+      if (!wk[b]) return -1;
+    }
+  }
+  int mask[BLK_MAXCOLS];
+  const int nv = wk[0]->num_vectors;
+  for (int c = 0; c < nv; c++) mask[c] = c < w;
+  for (int b = 0; b < 4; b++) gb_mv_set_mask_host(wk[b], mask);
+  gpu_MultiVector *r = wk[0], *z = wk[1], *p = wk[2], *q = wk[3];
+  blk_cols cx, cy, cr, cz, cp, cq;
+  gb_mv_fill_cols(X, &cx, 0);
+  gb_mv_fill_cols(Y, &cy, 0);
+  gb_mv_fill_cols(r, &cr, 0);
+  gb_mv_fill_cols(z, &cz, 0);
+  gb_mv_fill_cols(p, &cp, 0);
+  gb_mv_fill_cols(q, &cq, 0);
+  double *rho = op->coef, *rho2 = rho + BLK_MAXCOLS, *pq = rho2 + BLK_MAXCOLS,
+         *al = pq + BLK_MAXCOLS;
+  int idx[BLK_MAXCOLS];
+  for (int c = 0; c < w; c++) idx[c] = c;
+  const int dt = X->dtype;
+  const int f32 = dt == GPU_MV_FLOAT32;
+  long want = (op->n + 255) / 256, cap = (long)ctx->num_sms * 8 / w;
+  if (cap < 4) cap = 4;
+  if (want > cap) want = cap;
+  const dim3 grid((unsigned)want, w);
+#define PCG_COLS(mode, a, b, c, d, coef)                                                    \
+  do {                                                                                    \
+    if (f32)                                                                              \
+      pcg_cols_kernel<float><<<grid, 256, 0, S(ctx)>>>(op->n, mode, a, b, c, d, coef);    \
+    else                                                                                  \
+      pcg_cols_kernel<double><<<grid, 256, 0, S(ctx)>>>(op->n, mode, a, b, c, d, coef);   \
+    gb_count_launch(1);                                                                   \
+  } while (0)
+  // r = x ; z = M r ; p = z ; rho = r'z
+  if (gb_axpby(ctx, dt, op->n, 1.0, &cx, 0.0, &cr, w)) return -1;
+  if (op->prec) {
+    if (gb_operator_apply(op->prec, r, z)) return -1;
+  } else if (gb_axpby(ctx, dt, op->n, 1.0, &cr, 0.0, &cz, w)) {
+    return -1;
+  }
+  if (gb_axpby(ctx, dt, op->n, 1.0, &cz, 0.0, &cp, w)) return -1;
+  if (gb_dot_cols(ctx, dt, op->n, &cr, &cz, w, rho, idx)) return -1;
+  for (int it = 0; it < op->iters; it++) {
+    if (gb_operator_apply(op->inner, p, q)) return -1;
+    if (gb_dot_cols(ctx, dt, op->n, &cp, &cq, w, pq, idx)) return -1;
+    pcg_ratio_kernel<<<1, BLK_MAXCOLS, 0, S(ctx)>>>(w, rho, pq, al);
+    gb_count_launch(1);
+    PCG_COLS(it == 0 ? 0 : 1, cp, cq, cy, cr, al);  // y += alpha p ; r -= alpha q
+    if (it + 1 == op->iters) break;
+    if (op->prec) {
+      if (gb_operator_apply(op->prec, r, z)) return -1;
+    } else if (gb_axpby(ctx, dt, op->n, 1.0, &cr, 0.0, &cz, w)) {
+      return -1;
+    }
+    if (gb_dot_cols(ctx, dt, op->n, &cr, &cz, w, rho2, idx)) return -1;
+    pcg_ratio_kernel<<<1, BLK_MAXCOLS, 0, S(ctx)>>>(w, rho2, rho, al);  // beta
+    gb_count_launch(1);
+    PCG_COLS(2, cz, cz, cp, cp, al);  // p = z + beta p
+    double* t = rho;
+    rho = rho2;
+    rho2 = t;
+  }
+#undef PCG_COLS
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "pcg preconditioner");
 }

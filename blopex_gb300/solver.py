@@ -278,6 +278,15 @@ def Diagonal(ctx: Context, d) -> Operator:
     return Operator(ctx, h, len(d))
 
 
+def PCGPreconditioner(ctx: Context, A: Operator, M: Optional[Operator], iterations: int) -> Operator:
+    """T ~ inv(A) by `iterations` steps of CG preconditioned by M."""
+    h = ctx.lib.gpu_PCGPreconditionerCreate(ctx.handle, A.handle, M.handle if M is not None else None,
+                                            iterations)
+    op = Operator(ctx, h, A.n)
+    op.parts = (A, M)  # the device operator keeps raw pointers to these
+    return op
+
+
 class _Interp:
     """An mv_InterfaceInterpreter filled by GpuSetupInterpreter."""
 

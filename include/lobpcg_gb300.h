@@ -159,6 +159,15 @@ void gpu_OperatorDestroy(gpu_Operator* op);
 /* the callback to pass as operatorA/B/T together with the gpu_Operator* */
 void gpu_OperatorApply(void* op, void* X, void* Y);
 
+/* Inner conjugate-gradient preconditioner T ~ inv(A): applying it runs
+   `iterations` steps of CG on A Y = X from Y = 0, preconditioned by M (e.g.
+   gpu_DiagonalCreate of 1/diag(A); may be NULL), every column independently
+   and all columns in lockstep; in the dtype of the blocks.  The counterpart
+   of the CG-preconditioned LOBPCG of HYPRE's driver (-pcgitr,
+   blopex_hypre/krylov/HYPRE_lobpcg.c:317-320).  A and M must outlive it. */
+gpu_Operator* gpu_PCGPreconditionerCreate(gpu_Context* ctx, gpu_Operator* A, gpu_Operator* M,
+                                          int iterations);
+
 /* The two Gram matrices of an explicit-Gram LOBPCG step on the active
    columns of the blocks: G = [X R P]'[AX AR AP], H = [X R P]'[X R P], m x m
    (m = widths of X + R + P; R/P and AR/AP may be NULL), written to host

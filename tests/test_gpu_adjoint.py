@@ -239,3 +239,20 @@ def test_stencil5_gradcheck_64x64(ctx):
         fd = _richardson(exact, 1e-2)
         an = float((g * d).sum())
         assert abs(fd - an) <= RTOL * abs(an), (fd, an, abs(fd - an) / abs(an))
+
+
+def test_inner_cg_preconditioner_solve_and_gradient(ctx):
+    """LOBPCG preconditioned by an inner CG (the -pcgitr preconditioner) and
+    the flexible adjoint solve with the same preconditioner give the dense
+    reference's eigenvalues and gradient."""
+    ny, nx, k = 10, 12, 4
+    opts = AD.SolveOptions(k=k, atol=1e-11, maxit=2000, inner_cg=8)
+    v = torch.from_numpy(np.random.default_rng(5).standard_normal(nx * ny))
+    th = _theta(ny, nx, 3).requires_grad_(True)
+    L = _stencil5_loss(ctx, th, opts, v)
+    (g,) = torch.autograd.grad(L, th)
+    th2 = th.detach().clone().requires_grad_(True)
+    L2 = _stencil5_loss(ctx, th2, opts, v, device_solver=False)
+    (g2,) = torch.autograd.grad(L2, th2)
+    assert abs(L.item() - L2.item()) < 1e-9 * abs(L2.item())
+    assert ((g - g2).abs().max() / g2.abs().max()) < RTOL
