@@ -84,19 +84,31 @@ __global__ void __launch_bounds__(256) csr_kernel(long n, const int* __restrict_
 }
 
 // ------------------------------------------------------------ 7-point
+// One thread per cell, a CTA per 32 x 8 tile of a plane (the y-neighbours
+// of the tile's cells are mostly inside the tile: L1 hits; the tiles of the
+// neighbouring planes run 1 plane of CTAs earlier / later: L2 hits).  The
+// block columns go four at a time: the 28 neighbour loads of four columns
+// are issued before any of the four stores (Y may alias X as far as the
+// compiler knows, so loads would otherwise wait for the previous column's
+// store); the six face coefficients are read once per cell.
+#define ST_TX 32
+#define ST_TY 8
 template <typename T>
-__global__ void __launch_bounds__(256) st7_kernel(int nx, int ny, int nz, const T* __restrict__ cx,
-                                                  const T* __restrict__ cy,
-                                                  const T* __restrict__ cz, T shift, blk_cols X,
-                                                  blk_cols Y, int w)
+__global__ void __launch_bounds__(ST_TX* ST_TY) st7_kernel(int nx, int ny, int nz,
+                                                           const T* __restrict__ cx,
+                                                           const T* __restrict__ cy,
+                                                           const T* __restrict__ cz, T shift,
+                                                           blk_cols X, blk_cols Y, int w)
 {
-  long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  long n = (long)nx * ny * nz;
-  if (c >= n) return;
+  const int tiles_x = (nx + ST_TX - 1) / ST_TX, tiles_y = (ny + ST_TY - 1) / ST_TY;
+  const long b = blockIdx.x;
+  const int tile = (int)(b % ((long)tiles_x * tiles_y));
+  const int k = (int)(b / ((long)tiles_x * tiles_y));
+  const int i = (tile % tiles_x) * ST_TX + (int)(threadIdx.x % ST_TX);
+  const int j = (tile / tiles_x) * ST_TY + (int)(threadIdx.x / ST_TX);
+  if (i >= nx || j >= ny || k >= nz) return;
   const long plane = (long)nx * ny;
-  const int i = (int)(c % nx);
-  const int j = (int)((c / nx) % ny);
-  const int k = (int)(c / plane);
+  const long c = (long)i + (long)nx * j + plane * k;
   const long jk = (long)j + (long)ny * k;
   const T cw = cx[i + (long)(nx + 1) * jk];
   const T ce = cx[i + 1 + (long)(nx + 1) * jk];
@@ -105,16 +117,33 @@ __global__ void __launch_bounds__(256) st7_kernel(int nx, int ny, int nz, const 
   const T cb = cz[c];
   const T ct = cz[c + plane];
   const T dg = cw + ce + cs + cn + cb + ct + shift;
-  for (int col = 0; col < w; col++) {
-    const T* x = (const T*)X.col[col];
-    T v = dg * x[c];
-    if (i > 0) v -= cw * x[c - 1];
-    if (i < nx - 1) v -= ce * x[c + 1];
-    if (j > 0) v -= cs * x[c - nx];
-    if (j < ny - 1) v -= cn * x[c + nx];
-    if (k > 0) v -= cb * x[c - plane];
-    if (k < nz - 1) v -= ct * x[c + plane];
-    ((T*)Y.col[col])[c] = v;
+  // neighbour offsets, pointing at the cell itself (weight 0) off the grid
+  const long ow = i > 0 ? -1 : 0, oe = i < nx - 1 ? 1 : 0;
+  const long os = j > 0 ? -(long)nx : 0, on = j < ny - 1 ? (long)nx : 0;
+  const long ob = k > 0 ? -plane : 0, ot = k < nz - 1 ? plane : 0;
+  const T ww = i > 0 ? cw : T(0), we = i < nx - 1 ? ce : T(0);
+  const T ws = j > 0 ? cs : T(0), wn = j < ny - 1 ? cn : T(0);
+  const T wb = k > 0 ? cb : T(0), wt = k < nz - 1 ? ct : T(0);
+  constexpr int U = 4;
+  for (int col0 = 0; col0 < w; col0 += U) {
+    T v[U][7];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const T* x = (const T*)X.col[col0 + u < w ? col0 + u : col0];
+      v[u][0] = x[c];
+      v[u][1] = x[c + ow];
+      v[u][2] = x[c + oe];
+      v[u][3] = x[c + os];
+      v[u][4] = x[c + on];
+      v[u][5] = x[c + ob];
+      v[u][6] = x[c + ot];
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (col0 + u < w)
+        ((T*)Y.col[col0 + u])[c] = dg * v[u][0] - ww * v[u][1] - we * v[u][2] - ws * v[u][3] -
+                                   wn * v[u][4] - wb * v[u][5] - wt * v[u][6];
+    }
   }
 }
 
@@ -469,13 +498,17 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
         csr_kernel<double, double><<<blocks, 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx,
                                                                op->vals, xc, yc, w);
       break;
-    case OPK_ST7:
+    case OPK_ST7: {
+      const unsigned tb = (unsigned)(((op->nx + ST_TX - 1) / ST_TX) * ((op->ny + ST_TY - 1) / ST_TY) *
+                                     (long)op->nz);
       if (f32)
-        st7_kernel<float><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
-                                                      op->c32[2], (float)op->shift, xc, yc, w);
+        st7_kernel<float><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0],
+                                                            op->c32[1], op->c32[2], (float)op->shift,
+                                                            xc, yc, w);
       else
-        st7_kernel<double><<<blocks, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0], op->c[1],
-                                                       op->c[2], op->shift, xc, yc, w);
+        st7_kernel<double><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0],
+                                                             op->c[1], op->c[2], op->shift, xc, yc, w);
+    }
       break;
     case OPK_ST5:
       if (f32)

@@ -76,6 +76,9 @@ def _ops(ctx):
     out.append((S.CSRMatrix(ctx, rp, ci, va), O.csr(rp, ci, va), 315))
     cx, cy, cz = P.stencil7_coefficients(11, 6, 5, seed=2)
     out.append((S.Stencil7(ctx, cx, cy, cz, 0.3), O.stencil7(11, 6, 5, cx, cy, cz, 0.3), 330))
+    # several (x, y) tiles and z chunks of the blocked kernel, ragged edges
+    cx, cy, cz = P.stencil7_coefficients(37, 9, 70, seed=5)
+    out.append((S.Stencil7(ctx, cx, cy, cz, 0.0), O.stencil7(37, 9, 70, cx, cy, cz, 0.0), 23310))
     c = np.exp(rng.standard_normal((13, 17)))
     sx, sy = P.stencil5_from_cells(c)
     out.append((S.Stencil5(ctx, sx, sy, 0.1), O.stencil5(17, 13, sx, sy, 0.1), 221))
