@@ -517,6 +517,9 @@ def main():
         tot_m = sum(v["ms"] for v in kt_m.values()) or 1.0
         st = rm.stats
         mixed = {"seconds": tm, "seconds_per_iteration": tm / max(rm.iterations, 1),
+                 "seconds_fp32_phase": st["seconds_fp32"],
+                 "seconds_per_fp32_iteration": st["seconds_fp32"] / max(st["iterations_fp32"], 1),
+                 "seconds_fp64_phase": st["seconds_fp64"],
                  "flag": rm.flag, "iterations": rm.iterations,
                  "iterations_fp32": st["iterations_fp32"],
                  "iterations_compensated": st["iterations_compensated"],

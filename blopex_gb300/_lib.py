@@ -127,6 +127,7 @@ SIGNATURES = {
     "gpu_ContextSetProfiling": (c_int, [c_void_p, c_int]),
     "gpu_ContextKernelTimes": (c_int, [c_void_p, ctypes.POINTER(KernelTime), c_int]),
     "gpu_ContextResetKernelTimes": (None, [c_void_p]),
+    "gpu_ContextTrim": (None, [c_void_p]),
     "gpu_KernelLaunchCount": (c_longlong, []),
     "gpu_MultiVectorCreate": (c_void_p, [c_void_p, c_long, c_int, c_int]),
     "gpu_MultiVectorWrapDevice": (c_void_p, [c_void_p, c_void_p, c_long, c_long, c_int, c_int]),

@@ -197,10 +197,45 @@ extern "C" void gpu_ContextDestroy(gpu_Context* ctx)
   free(ctx->prof_pool);
   free(ctx->prof_pending);
   if (ctx->work) cudaFree(ctx->work);
+  gpu_ContextTrim(ctx);
   if (ctx->dcount) cudaFree(ctx->dcount);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->owns_stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
   free(ctx);
+}
+
+extern "C" void* gb_pool_get(gpu_Context* ctx, size_t bytes)
+{
+  for (int i = 0; i < ctx->pool_n; i++)
+    if (ctx->pool_bytes[i] == bytes) {
+      void* p = ctx->pool_ptr[i];
+      ctx->pool_n--;
+      ctx->pool_ptr[i] = ctx->pool_ptr[ctx->pool_n];
+      ctx->pool_bytes[i] = ctx->pool_bytes[ctx->pool_n];
+      return p;
+    }
+  return gb_device_alloc(ctx, bytes);
+}
+
+extern "C" void gb_pool_put(gpu_Context* ctx, void* p, size_t bytes)
+{
+  if (!p) return;
+  if (ctx->pool_n < GB_POOL_MAX) {
+    ctx->pool_ptr[ctx->pool_n] = p;
+    ctx->pool_bytes[ctx->pool_n] = bytes;
+    ctx->pool_n++;
+    return;
+  }
+  cudaStreamSynchronize((cudaStream_t)ctx->stream);
+  gb_device_free(p);
+}
+
+extern "C" void gpu_ContextTrim(gpu_Context* ctx)
+{
+  if (!ctx || ctx->pool_n == 0) return;
+  cudaStreamSynchronize((cudaStream_t)ctx->stream);
+  for (int i = 0; i < ctx->pool_n; i++) gb_device_free(ctx->pool_ptr[i]);
+  ctx->pool_n = 0;
 }
 
 extern "C" void* gpu_ContextStream(gpu_Context* ctx) { return ctx ? ctx->stream : NULL; }

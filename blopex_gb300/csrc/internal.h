@@ -14,6 +14,7 @@ extern "C" {
 
 /* widest block handed to one kernel: [X R P] for k = 128 */
 #define BLK_MAXCOLS 384
+#define GB_POOL_MAX 64
 
 /* Column pointer table passed by value to the block kernels: logical
    column c of an operand lives at col[c] (device address, `len` rows). */
@@ -61,9 +62,20 @@ struct gpu_Context {
   int prof_npool;
   lobpcg_gpu_kernel_time prof[GB_K_COUNT];
   /* device counters: [0] FP32 Jacobi sweeps, [1] largest refinement
-     cluster, [2] FP64 fallback solves, [3] Rayleigh-Ritz calls */
+     cluster, [2] FP64 fallback solves, [3] Rayleigh-Ritz calls, [4] graded
+     pencils, [5] tensor-core kernel error word */
   int* dcount;
+  /* device buffers of the solver's internal blocks, kept across solves (all
+     work is ordered on ctx->stream, so a returned buffer can be handed out
+     again at once); freed by gpu_ContextTrim / gpu_ContextDestroy */
+  int pool_n;
+  void* pool_ptr[GB_POOL_MAX];
+  size_t pool_bytes[GB_POOL_MAX];
 };
+
+/* internal block storage from / back to the context's pool */
+void* gb_pool_get(gpu_Context* ctx, size_t bytes);
+void gb_pool_put(gpu_Context* ctx, void* p, size_t bytes);
 
 /* error helpers (context.cu) */
 int gb_fail(gpu_Context* ctx, const char* fmt, ...);

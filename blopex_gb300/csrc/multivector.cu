@@ -88,7 +88,11 @@ extern "C" gpu_MultiVector* gpu_MultiVectorWrapDevice(gpu_Context* ctx, void* da
 extern "C" void gpu_MultiVectorDestroy(gpu_MultiVector* x)
 {
   if (!x) return;
-  if (x->owns_data && x->data) {
+  if (x->owns_data == 2 && x->data) {
+    // internal block: its storage goes back to the context's pool
+    gb_pool_put(x->ctx, x->data,
+                esize(x->dtype) * (size_t)x->ld * (size_t)(x->num_vectors > 0 ? x->num_vectors : 1));
+  } else if (x->owns_data && x->data) {
     cudaStreamSynchronize((cudaStream_t)x->ctx->stream);
     gb_device_free(x->data);
   }
@@ -97,9 +101,25 @@ extern "C" void gpu_MultiVectorDestroy(gpu_MultiVector* x)
   free(x);
 }
 
+// the solver's internal blocks: storage from the context's pool (no
+// cudaMalloc / cudaFree per solve for repeated solves of one shape)
 extern "C" gpu_MultiVector* gb_mv_create_like(const gpu_MultiVector* x, int dtype)
 {
-  return gpu_MultiVectorCreate(x->ctx, x->size, x->num_vectors, dtype);
+  gpu_Context* ctx = x->ctx;
+  const int k = x->num_vectors;
+  gpu_MultiVector* y = mv_alloc(ctx, x->size, k, dtype);
+  if (!y) return NULL;
+  const size_t bytes = esize(dtype) * (size_t)y->ld * (size_t)(k > 0 ? k : 1);
+  y->data = gb_pool_get(ctx, bytes);
+  if (!y->data) {
+    free(y->active);
+    gb_device_free(y->active_dev);
+    free(y);
+    return NULL;
+  }
+  cudaMemsetAsync(y->data, 0, bytes, (cudaStream_t)ctx->stream);
+  y->owns_data = 2;
+  return y;
 }
 
 extern "C" int gb_mv_fill_cols(const gpu_MultiVector* x, blk_cols* t, int offset)

@@ -79,6 +79,9 @@ gpu_Context* gpu_ContextCreate(int device, void* stream);
 void gpu_ContextDestroy(gpu_Context* ctx);
 void* gpu_ContextStream(gpu_Context* ctx);
 int gpu_ContextSynchronize(gpu_Context* ctx);
+/* free the device storage the context keeps for the solver's internal blocks
+   between solves (it reuses it when the next solve has the same shapes) */
+void gpu_ContextTrim(gpu_Context* ctx);
 void gpu_ContextGetOptions(gpu_Context* ctx, lobpcg_gpu_options* opt);
 int gpu_ContextSetOptions(gpu_Context* ctx, const lobpcg_gpu_options* opt);
 void gpu_ContextGetStats(gpu_Context* ctx, lobpcg_gpu_stats* stats);
