@@ -176,13 +176,16 @@ def roofline_entry(name, v, hbm_peak, fp64_peak, traffic, fp64_arith=True, tf32_
     return out
 
 
-def load_traffic():
-    """DRAM bytes per launch from the committed ncu summary (profiles/)."""
+def load_traffic(config: str):
+    """DRAM bytes per launch of a kernel class on this workload, from the
+    committed ncu summary (profiles/traffic.json); entries name the workload
+    they were captured on."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f)
+            entries = json.load(f)
     except (OSError, ValueError):
         return {}
+    return {k: v for k, v in entries.items() if v.get("config") == config}
 
 
 def build_problem(cfg, grid=None):
@@ -495,7 +498,7 @@ def main():
     pk, pk_kind = peaks()
     fp64_peak = fp64_peak_tflops(torch)
     tf32_peak = pk["bf16_tflops"] / 2.0
-    traffic = load_traffic()
+    traffic = load_traffic(args.config)
 
     # the mixed-precision arm on the same problem (one solve, timed, with
     # its own kernel breakdown)
