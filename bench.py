@@ -369,7 +369,9 @@ def metric_name(cfg):
 
 
 def config_block(cfg, args):
-    return {"workload": cfg["label"], "mode": args.mode, "n": int(np.prod(cfg["grid"])),
+    return {"workload": cfg["label"] + (f" [preconditioner: {args.precond[3:]} inner CG steps]"
+                                        if args.precond else ""),
+            "mode": args.mode, "n": int(np.prod(cfg["grid"])),
             "k": cfg["k"], "maxit": args.maxit or cfg["maxit"], "tol": cfg["tol"],
             "l2": "inputs larger than L2 (X alone is n*k*8 bytes)" if np.prod(cfg["grid"]) *
                   cfg["k"] * 8 > 129e6 else "inputs smaller than L2", "parallelism":
@@ -385,6 +387,10 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--mode", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--maxit", type=int, default=0, help="override maxit (exploration only)")
+    ap.add_argument("--precond", default="",
+                    help="'pcgN': precondition with N inner CG steps (Jacobi inside) instead of "
+                         "Jacobi alone")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end repetition")
     ap.add_argument("--grid", type=int, default=0,
                     help="override the grid edge (small cases for profiling only)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision arm")
@@ -430,6 +436,8 @@ def main():
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     A = S.CSRMatrix(ctx, *op[1]) if op[0] == "csr" else S.Stencil7(ctx, *op[1])
     T = S.Diagonal(ctx, tdiag) if tdiag is not None else None
+    if args.precond.startswith("pcg"):
+        T = S.PCGPreconditioner(ctx, A, T, int(args.precond[3:]))
     X = S.MultiVector(ctx, n, k)
     if x0 is not None:
         X0 = S.MultiVector.from_host(ctx, x0)
@@ -480,7 +488,7 @@ def main():
     pinned_out = torch.empty(n * k, dtype=torch.float64).pin_memory()
     ctx.set_options(precision=S.FP64 if args.mode == "fp64" else S.MIXED)
     e2e_times = []
-    for _ in range(max(1, args.steps)):
+    for _ in range(0 if args.no_e2e else max(1, args.steps)):
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -489,8 +497,8 @@ def main():
                                    history=False)
         X.download_ptr(pinned_out.data_ptr(), n)
         e2e_times.append(time.perf_counter() - t0)
-    e2e = statistics.median(e2e_times)
-    if dist is not None:
+    e2e = statistics.median(e2e_times) if e2e_times else None
+    if dist is not None and e2e is not None:
         t = torch.tensor([e2e], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e = float(t.item())
@@ -567,8 +575,9 @@ def main():
                                                              fp64_peak, traffic),
             "kernels": kernels,
             "mixed": mixed,
-            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": n * k * 8,
-                    "d2h_bytes_per_step": n * k * 8 + 2 * k * 8},
+            "e2e": None if e2e is None else {"value": e2e, "unit": "s",
+                                             "h2d_bytes_per_step": n * k * 8,
+                                             "d2h_bytes_per_step": n * k * 8 + 2 * k * 8},
             "gpu_launches": int(launches),
             "clocks": clocks}
     if rank == 0 and not args.no_cpu:

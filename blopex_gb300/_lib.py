@@ -27,7 +27,8 @@ class BlasLapack(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("compensated_below", c_double), ("fp64_below", c_double),
                 ("fp32_stall", c_int), ("tensor_cores", c_int), ("potrf_fail_at", c_int),
-                ("sygv_fail_at", c_int), ("rr_method", c_int)]
+                ("sygv_fail_at", c_int), ("explicit_pivot_below", c_double),
+                ("accum64", c_int), ("rr_method", c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -37,7 +38,7 @@ class Stats(ctypes.Structure):
                 ("seconds_fp64", c_double), ("final_max_residual", c_double),
                 ("rr_calls", c_int), ("rr_jacobi32_sweeps", c_int), ("rr_max_cluster", c_int),
                 ("rr_fallbacks", c_int), ("rr_graded", c_int),
-                ("explicit_undos", c_int)]
+                ("explicit_undos", c_int), ("explicit_p_drops", c_int)]
 
 
 class KernelTime(ctypes.Structure):

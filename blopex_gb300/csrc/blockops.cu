@@ -360,19 +360,31 @@ extern "C" int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* 
 }
 
 // fused residual R = lambda*BX - AX with squared column norms
-template <typename T>
+template <typename T, int OUT32>
+struct rr_out {
+  typedef T type;
+};
+template <>
+struct rr_out<double, 1> {
+  typedef float type;
+};
+
+template <typename T, int OUT32 = 0>
 __global__ void residual_partial_kernel(blk_cols BX, blk_cols AX, const double* __restrict__ lambda,
                                         idx_table idx, blk_cols R, long n,
                                         double* __restrict__ partial)
 {
+  // T: arithmetic and input type; the residual is stored as TO (FP32 for the
+  // FP64-accumulated explicit phase: its norm is taken before the rounding)
+  using TO = typename rr_out<T, OUT32>::type;
   const T* bx = (const T*)BX.col[blockIdx.y];
   const T* ax = (const T*)AX.col[blockIdx.y];
-  T* rr = (T*)R.col[blockIdx.y];
+  TO* rr = (TO*)R.col[blockIdx.y];
   const T lam = (T)lambda[idx.v[blockIdx.y]];
   double s = 0.0;
   for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
     T v = lam * bx[r] - ax[r];
-    rr[r] = v;
+    rr[r] = (TO)v;
     s += (double)v * (double)v;
   }
   __shared__ double red[256];
@@ -400,12 +412,61 @@ extern "C" int gb_residual(gpu_Context* ctx, int dtype, long n, const blk_cols* 
   gb_prof_begin(ctx, &pr, GB_K_RESID);
   if (dtype == GPU_MV_FLOAT64)
     residual_partial_kernel<double><<<grid, 256, 0, S(ctx)>>>(*BX, *AX, lambda, t, *R, n, partial);
-  else
+  else if (dtype == GPU_MV_FLOAT32)
     residual_partial_kernel<float><<<grid, 256, 0, S(ctx)>>>(*BX, *AX, lambda, t, *R, n, partial);
+  else  // FP64 inputs, FP32 residual
+    residual_partial_kernel<double, 1><<<grid, 256, 0, S(ctx)>>>(*BX, *AX, lambda, t, *R, n, partial);
   dot_reduce_kernel<<<(w + 63) / 64, 64, 0, S(ctx)>>>(partial, nb, t, w, norm2);
-  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * w * 3, 4.0 * n * w);
+  gb_prof_end(ctx, &pr, (dtype == GPU_MV_FLOAT32 ? 12.0 : (dtype == GPU_MV_FLOAT64 ? 24.0 : 20.0)) * n * w,
+              4.0 * n * w);
   gb_count_launch(2);
   return CUDA_LAUNCH_CHECK(ctx, "residual");
+}
+
+// Y64 = X64 + D (D FP32), and D <- (float) Y64: the FP64-accumulated block
+// update of the explicit phase (the correction carries FP32 rounding
+// relative to its own size) and its FP32 shadow
+__global__ void acc64_kernel(blk_cols X, blk_cols D, blk_cols Y, long n)
+{
+  const double* x = (const double*)X.col[blockIdx.y];
+  float* d = (float*)D.col[blockIdx.y];
+  double* y = (double*)Y.col[blockIdx.y];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    const double v = x[r] + (double)d[r];
+    y[r] = v;
+    d[r] = (float)v;
+  }
+}
+
+extern "C" int gb_accumulate64(gpu_Context* ctx, long n, const blk_cols* X64, const blk_cols* D32,
+                               const blk_cols* Y64, int w)
+{
+  if (w <= 0 || n <= 0) return 0;
+  dim3 grid(row_blocks(ctx, n, w), w);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_BLAS1);
+  acc64_kernel<<<grid, 256, 0, S(ctx)>>>(*X64, *D32, *Y64, n);
+  gb_prof_end(ctx, &pr, 24.0 * n * w, (double)n * w);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "accumulate64");
+}
+
+__global__ void rayleigh_kernel(int w, const double* num, const double* den, double* lam)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < w) lam[i] = den[i] > 0.0 ? num[i] / den[i] : 0.0;
+}
+
+extern "C" int gb_rayleigh_quotients(gpu_Context* ctx, int dtype, long n, const blk_cols* X,
+                                     const blk_cols* AX, int w, double* scratch, double* lam)
+{
+  int idx[BLK_MAXCOLS];
+  for (int c = 0; c < w; c++) idx[c] = c;
+  if (gb_dot_cols(ctx, dtype, n, X, AX, w, scratch, idx)) return -1;
+  if (gb_dot_cols(ctx, dtype, n, X, X, w, scratch + w, idx)) return -1;
+  rayleigh_kernel<<<(w + 127) / 128, 128, 0, S(ctx)>>>(w, scratch, scratch + w, lam);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "rayleigh quotients");
 }
 
 template <typename TI, typename TO>

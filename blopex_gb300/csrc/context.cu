@@ -54,7 +54,9 @@ static void default_options(lobpcg_gpu_options* o)
   memset(o, 0, sizeof(*o));
   o->precision = LOBPCG_GPU_FP64;
   o->compensated_below = 1e-6;
-  o->fp64_below = 2e-6;
+  o->fp64_below = 0.0;
+  o->accum64 = 1;
+  o->explicit_pivot_below = 1e-6;
   o->fp32_stall = 20;
   o->tensor_cores = 1;
 }

@@ -116,6 +116,106 @@ __global__ void __launch_bounds__(DENSE_THREADS) cholqr_factor_kernel(double* A,
   }
 }
 
+// Cholesky of a Gram block that may be (numerically) rank deficient: a
+// column whose pivot falls below tol times its diagonal is dropped (its row
+// of U is zeroed with a unit diagonal, dropped[j] = 1); then A <- inv(U)
+// with the dropped columns zeroed, so that the dropped directions leave the
+// basis.  *ndrop = number of dropped columns.
+__global__ void __launch_bounds__(DENSE_THREADS) chol_deflate_kernel(double* A, int ld, int m,
+                                                                     double tol, int* dropped,
+                                                                     int* ndrop, double* W)
+{
+  __shared__ int s_drop;
+  __shared__ int s_cnt;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) s_cnt = 0;
+  for (int j = 0; j < m; j++) {
+    if (tid == 0) {
+      const double d0 = A[j + (size_t)j * ld];
+      double s = d0;
+      for (int p = 0; p < j; p++) {
+        const double u = A[p + (size_t)j * ld];
+        s -= u * u;
+      }
+      s_drop = !(s > tol * d0) || !(d0 > 0.0);
+      A[j + (size_t)j * ld] = s_drop ? 1.0 : sqrt(s);
+      dropped[j] = s_drop;
+      s_cnt += s_drop;
+    }
+    __syncthreads();
+    const int drop = s_drop;
+    const double ujj = A[j + (size_t)j * ld];
+    for (int i = j + 1 + tid; i < m; i += nt) {
+      double v = 0.0;
+      if (!drop) {
+        v = A[j + (size_t)i * ld];
+        for (int p = 0; p < j; p++) v -= A[p + (size_t)j * ld] * A[p + (size_t)i * ld];
+        v /= ujj;
+      }
+      A[j + (size_t)i * ld] = v;
+    }
+    __syncthreads();
+  }
+  for (int j = tid; j < m; j += nt) {
+    double* x = W + (size_t)j * m;
+    for (int i = m - 1; i > j; i--) x[i] = 0.0;
+    x[j] = 1.0 / A[j + (size_t)j * ld];
+    for (int i = j - 1; i >= 0; i--) {
+      double t = 0.0;
+      for (int l = i + 1; l <= j; l++) t += A[i + (size_t)l * ld] * x[l];
+      x[i] = -t / A[i + (size_t)i * ld];
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e % m, j = e / m;
+    A[i + (size_t)j * ld] = (i <= j && !dropped[j]) ? W[(size_t)j * m + i] : 0.0;
+  }
+  if (tid == 0) *ndrop = s_cnt;
+}
+
+extern "C" int gb_chol_deflate(gpu_Context* ctx, double* A, int ld, int m, double tol, int* dropped,
+                               int* ndrop)
+{
+  double* W = (double*)gb_workspace(ctx, sizeof(double) * (size_t)m * m + 64);
+  if (!W) return -1;
+  chol_deflate_kernel<<<1, DENSE_THREADS, 0, S(ctx)>>>(A, ld, m, tol, dropped, ndrop, W);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "chol_deflate");
+}
+
+// rows / columns off + j of the pencil (G2, H2) for dropped[j]: decoupled,
+// H2_jj = 1 and G2_jj = 2 max_{i<kx} |G2_ii| + 1.  By interlacing with the
+// first kx coordinates (H2 = I on them) the kx smallest eigenvalues are at
+// most max_{i<kx} G2_ii, so those coordinates take no part in the wanted
+// eigenvectors, and the pencil's norm grows by at most a factor ~2.
+__global__ void deflate_pencil_kernel(double* G, double* H, int ld, int mtot, int off, int m,
+                                      const int* dropped, int kx)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * mtot) return;
+  const int j = e % m, o = e / m;
+  if (!dropped[j]) return;
+  double big = 0.0;
+  for (int i = 0; i < kx; i++) big = fmax(big, fabs(G[i + (size_t)i * ld]));
+  big = 2.0 * big + 1.0;
+  const int a = off + j;
+  const double g = (o == a) ? big : 0.0, h = (o == a) ? 1.0 : 0.0;
+  G[a + (size_t)o * ld] = g;
+  G[o + (size_t)a * ld] = g;
+  H[a + (size_t)o * ld] = h;
+  H[o + (size_t)a * ld] = h;
+}
+
+extern "C" int gb_deflate_pencil(gpu_Context* ctx, double* G, double* H, int ld, int mtot, int off,
+                                 int m, const int* dropped, int kx)
+{
+  if (m <= 0) return 0;
+  deflate_pencil_kernel<<<(m * mtot + 255) / 256, 256, 0, S(ctx)>>>(G, H, ld, mtot, off, m, dropped, kx);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "deflate_pencil");
+}
+
 extern "C" int gb_cholqr_factor(gpu_Context* ctx, double* A, int ld, int m, int* info)
 {
   double* W = (double*)gb_workspace(ctx, sizeof(double) * (size_t)m * m + 64);
@@ -407,6 +507,20 @@ extern "C" int gb_small_identity(gpu_Context* ctx, double* A, int ld, int h, int
   small_identity_kernel<<<small_blocks(h * w), 256, 0, S(ctx)>>>(A, ld, h, w);
   gb_count_launch(1);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "identity");
+}
+
+__global__ void small_add_diag_kernel(double* A, int ld, int m, double alpha)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) A[i + (size_t)i * ld] += alpha;
+}
+
+extern "C" int gb_small_add_diag(gpu_Context* ctx, double* A, int ld, int m, double alpha)
+{
+  if (m <= 0) return 0;
+  small_add_diag_kernel<<<(m + 255) / 256, 256, 0, S(ctx)>>>(A, ld, m, alpha);
+  gb_count_launch(1);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "add_diag");
 }
 
 extern "C" int gb_small_diag(gpu_Context* ctx, double* A, int ld, int m, const double* d)

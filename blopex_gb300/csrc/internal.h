@@ -123,9 +123,27 @@ int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X, const bl
 /* Y(:,j) (dtype_y) = X(:,j) (dtype_x), converting precision */
 int gb_convert(gpu_Context* ctx, long n, int dtype_x, const blk_cols* X, int dtype_y,
                const blk_cols* Y, int w);
-/* fused residual: R(:,j) = lambda[idx[j]] * BX(:,j) - AX(:,j); norm2[idx[j]] = |R(:,j)|^2 */
+/* fused residual: R(:,j) = lambda[idx[j]] * BX(:,j) - AX(:,j); norm2[idx[j]] = |R(:,j)|^2.
+   dtype GB_RESID_64TO32: FP64 BX, AX and an FP32 R (norms from the FP64 values) */
+#define GB_RESID_64TO32 3
 int gb_residual(gpu_Context* ctx, int dtype, long n, const blk_cols* BX, const blk_cols* AX,
                 const double* lambda, const int* idx, const blk_cols* R, int w, double* norm2);
+/* Y64 = X64 + D32 and D32 <- (float) Y64, columnwise */
+int gb_accumulate64(gpu_Context* ctx, long n, const blk_cols* X64, const blk_cols* D32,
+                    const blk_cols* Y64, int w);
+/* lam[j] = X(:,j)'AX(:,j) / X(:,j)'X(:,j) (device; scratch: 2w doubles) */
+int gb_rayleigh_quotients(gpu_Context* ctx, int dtype, long n, const blk_cols* X,
+                          const blk_cols* AX, int w, double* scratch, double* lam);
+/* Cholesky with deflation of columns whose pivot ratio is below tol; A <-
+   inv(U) with the dropped columns zeroed; dropped[j] (device) marks them,
+   *ndrop (device) counts them */
+int gb_chol_deflate(gpu_Context* ctx, double* A, int ld, int m, double tol, int* dropped, int* ndrop);
+/* decouple the dropped coordinates off + j of a pencil (H2_jj = 1, G2_jj above
+   the kx smallest eigenvalues) */
+int gb_deflate_pencil(gpu_Context* ctx, double* G, double* H, int ld, int mtot, int off, int m,
+                      const int* dropped, int kx);
+/* A(i,i) += alpha for i < m (device small matrix) */
+int gb_small_add_diag(gpu_Context* ctx, double* A, int ld, int m, double alpha);
 /* drand48-compatible fill of column-major storage, columns listed in idx */
 int gb_drand48_fill(gpu_Context* ctx, int dtype, void* data, long n, long ld, const int* idx,
                     int w, unsigned int seed);

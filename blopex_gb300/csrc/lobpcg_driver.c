@@ -566,10 +566,6 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
 
 /* ------------------------------------------------- explicit-Gram phase */
 
-/* the FP32 Gram matrices carry relative errors down to ~1e-6 (compensated)
-   and ~1e-4 (TF32): a basis vector whose squared sine to the span of the
-   previous ones is below this is not resolved, and P is dropped */
-#define EXPLICIT_PIVOT_BELOW 1e-6
 /* a step whose largest active residual grows by more than this is undone */
 #define EXPLICIT_JUMP 20.0
 
@@ -594,7 +590,17 @@ typedef struct {
   gpu_MultiVector *Xn, *AXn, *BXn, *Pn, *APn, *BPn;
   double *G, *H, *Gs, *Hs, *T, *G2, *H2, *tmp, *d, *w;
   int* infos; /* device: 3 Cholesky status words */
+  /* FP64 accumulation: X and AX in FP64 (double-buffered), the caller's
+     FP64 block that receives X at the end, scratch for Rayleigh quotients */
+  gpu_MultiVector *X64[2], *AX64[2], *Xout;
+  double* rq;
+  int wrote_x64;
+  int* pdrop; /* device: P columns dropped by the deflating Cholesky */
 } explicit_bufs;
+
+/* exact A X in FP64 every this many FP64-accumulated steps (in between, AX is
+   updated by FP32 corrections like X) */
+#define ACC64_REFRESH 8
 
 /* Block-orthonormalise the explicit pencil on the small side: with U_b the
    upper Cholesky factor of the b-th diagonal block of H (b = X, R, P),
@@ -610,24 +616,36 @@ static int explicit_orthonormalise(solver_t* s, explicit_bufs* eb, int nR, int n
   for (int b = 0; b < 3; b++) {
     if (sz[b] == 0) continue;
     double* Tb = eb->T + off[b] + (size_t)off[b] * k3;
-    /* T_bb <- H_bb, then inv(chol(H_bb)) in place */
+    /* T_bb <- H_bb, then inv(chol(H_bb)) in place; P's block drops only the
+       columns that are not resolved (directions already in span [X R]) */
     if (gb_small_copy(s->ctx, eb->H + off[b] + (size_t)off[b] * k3, k3, Tb, k3, sz[b], sz[b]))
       return -1;
-    if (gb_cholqr_factor(s->ctx, Tb, k3, sz[b], eb->infos + b)) return -1;
+    if (b == 2) {
+      if (gb_chol_deflate(s->ctx, Tb, k3, sz[b], s->ctx->opt.explicit_pivot_below, eb->pdrop,
+                          eb->infos + 3))
+        return -1;
+    } else if (gb_cholqr_factor(s->ctx, Tb, k3, sz[b], eb->infos + b)) {
+      return -1;
+    }
   }
-  int* hinfo = (int*)gb_pinned(s->ctx, sizeof(int) * 3);
-  if (!hinfo || gb_memcpy_d2h(s->ctx, hinfo, eb->infos, sizeof(int) * 3)) return -1;
-  *bad = (sz[0] && hinfo[0] ? 1 : 0) | (sz[1] && hinfo[1] ? 2 : 0) | (sz[2] && hinfo[2] ? 4 : 0);
+  int* hinfo = (int*)gb_pinned(s->ctx, sizeof(int) * 4);
+  if (!hinfo || gb_memcpy_d2h(s->ctx, hinfo, eb->infos, sizeof(int) * 4)) return -1;
+  const int ndrop = sz[2] ? hinfo[3] : 0;
+  *bad = (sz[0] && hinfo[0] ? 1 : 0) | (sz[1] && hinfo[1] ? 2 : 0) | (sz[2] && ndrop == sz[2] ? 4 : 0);
   if (*bad) return 0;
+  s->ctx->stats.explicit_p_drops += ndrop;
   /* G2 = T' G T, H2 = T' H T */
   if (gb_small_gemm(s->ctx, eb->G, k3, 0, eb->T, k3, 0, eb->tmp, k3, m, m, m)) return -1;
   if (gb_small_gemm(s->ctx, eb->T, k3, 1, eb->tmp, k3, 0, eb->G2, k3, m, m, m)) return -1;
   if (gb_small_gemm(s->ctx, eb->H, k3, 0, eb->T, k3, 0, eb->tmp, k3, m, m, m)) return -1;
   if (gb_small_gemm(s->ctx, eb->T, k3, 1, eb->tmp, k3, 0, eb->H2, k3, m, m, m)) return -1;
+  if (ndrop && gb_deflate_pencil(s->ctx, eb->G2, eb->H2, k3, m, off[2], sz[2], eb->pdrop, k))
+    return -1;
   return 0;
 }
 
-/* R(0:nR) = BX(act) diag(lambda(act)) - AX(act), norms of those columns */
+/* R(0:nR) = BX(act) diag(lambda(act)) - AX(act), norms of those columns
+   (from FP64 BX, AX into the FP32 R when they are FP64) */
 static int explicit_residual(solver_t* s, gpu_MultiVector* X, gpu_MultiVector* AX,
                              gpu_MultiVector* BX, const int* act, int nR)
 {
@@ -636,7 +654,8 @@ static int explicit_residual(solver_t* s, gpu_MultiVector* X, gpu_MultiVector* A
   cols_idx(AX, act, nR, &ax, 0);
   cols_idx(s->R, NULL, nR, &r, 0);
   (void)X;
-  if (gb_residual(s->ctx, s->dt, s->n, &bx, &ax, s->lam, act, &r, nR, s->norm2)) return -1;
+  const int dt = (AX->dtype == GPU_MV_FLOAT64 && s->R->dtype == GPU_MV_FLOAT32) ? GB_RESID_64TO32 : s->dt;
+  if (gb_residual(s->ctx, dt, s->n, &bx, &ax, s->lam, act, &r, nR, s->norm2)) return -1;
   double* tmp = (double*)gb_pinned(s->ctx, sizeof(double) * s->k);
   if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->norm2, sizeof(double) * s->k)) return -1;
   for (int c = 0; c < nR; c++) s->h_norm[act[c]] = sqrt(fabs(tmp[act[c]]));
@@ -686,6 +705,30 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
   for (int i = 0; i < k; i++) prev_act[i] = i;  /* phase_setup left R for all columns */
   gb_mv_set_mask_host(X, NULL);
   gb_mv_set_mask_host(AX, NULL);
+  /* FP64 accumulation (with the tensor-core kernels and B = I): X and AX are
+     carried in FP64 and every step adds an FP32 correction computed from the
+     FP32 shadows X, AX; residuals and Ritz values (Rayleigh quotients) come
+     from the FP64 pair, so the phase is not held at the FP32 rounding floor of
+     the blocks.  The Gram products still limit it to ~1e-7 of the spectrum's
+     scale, below which the FP64 iteration takes over. */
+  const int acc64 = tc_ok && eb->X64[0] && eb->X64[1] && eb->AX64[0] && eb->AX64[1];
+  gpu_MultiVector *X64 = eb->X64[0], *X64n = eb->X64[1], *AX64 = eb->AX64[0], *AX64n = eb->AX64[1];
+  int refresh = 0;
+  gpu_MultiVector* t64;
+  if (acc64) {
+    gpu_MultiVector* b4[4] = {X64, X64n, AX64, AX64n};
+    for (int b = 0; b < 4; b++) gb_mv_set_mask_host(b4[b], NULL);
+    if (d_copy(s, X, X64) || d_apply(s, s->A, s->Adata, X64, AX64)) return -2;
+    blk_cols c64, a64;
+    cols_idx(X64, NULL, k, &c64, 0);
+    cols_idx(AX64, NULL, k, &a64, 0);
+    if (gb_rayleigh_quotients(s->ctx, GPU_MV_FLOAT64, s->n, &c64, &a64, k, eb->rq, s->lam) ||
+        fetch_lambda(s))
+      return -2;
+    for (int i = 0; i < k; i++) prev_act[i] = i;
+    set_prefix(R, k);
+    if (explicit_residual(s, X64, AX64, X64, prev_act, k)) return -2;
+  }
 
   for (*it = ctl->it_base + 1; *it <= ctl->maxit; (*it)++) {
     nR = 0;
@@ -729,7 +772,9 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     }
     /* the residual block must hold exactly the active columns */
     if (nR != prev_nR || memcmp(act, prev_act, sizeof(int) * nR)) {
-      if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
+      if (acc64 ? explicit_residual(s, X64, AX64, X64, act, nR)
+                : explicit_residual(s, X, AX, BX, act, nR))
+        return -2;
     }
     set_prefix(R, nR);
     set_prefix(AR, nR);
@@ -789,6 +834,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       }
       if (bad & 4) {
         use_p = 0;
+        s->ctx->stats.explicit_p_drops += nP;
         if (explicit_orthonormalise(s, eb, nR, 0, &bad)) return -2;
         if (bad) {
           ctl->handed_over = 1;
@@ -800,10 +846,13 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         if (gb_small_copy(s->ctx, eb->G2, k3, eb->Gs, k3, mm, mm) ||
             gb_small_copy(s->ctx, eb->H2, k3, eb->Hs, k3, mm, mm))
           return -2;
-        if (gb_sygv(s->ctx, eb->Gs, eb->Hs, k3, mm, k, eb->w, s->info, EXPLICIT_PIVOT_BELOW) || read_info(s, &info))
+        if (gb_sygv(s->ctx, eb->Gs, eb->Hs, k3, mm, k, eb->w, s->info,
+                    s->ctx->opt.explicit_pivot_below) ||
+            read_info(s, &info))
           return -2;
         if (info == 0 || use_p == 0) break;
         use_p = 0;
+        s->ctx->stats.explicit_p_drops++;
         if (explicit_orthonormalise(s, eb, nR, 0, &bad)) return -2;
         if (bad) break;
       }
@@ -819,6 +868,9 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       if (gb_memcpy_d2d(s->ctx, eb->d, s->lam, sizeof(double) * k)) return -2;
       if (gb_memcpy_d2d(s->ctx, s->lam, eb->w, sizeof(double) * k)) return -2;
 
+      /* FP64 accumulation: the FP32 kernels produce the correction
+         X (C_X - I) + P, added to the FP64 block below */
+      if (acc64 && gb_small_add_diag(s->ctx, eb->Gs, k3, k, -1.0)) return -2;
       /* P = [R P(act)] C_RP ; X = X C_X + P, and the A / B images */
       const double* cX = eb->Gs;
       const double* cRP = eb->Gs + k;
@@ -840,6 +892,29 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
           if (gb_bymat(s->ctx, s->dt, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
           if (gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
         }
+      }
+      if (acc64) {
+        blk_cols x0, xd, x1;
+        cols_idx(X64, NULL, k, &x0, 0);
+        cols_idx(Xn, NULL, k, &xd, 0);
+        cols_idx(X64n, NULL, k, &x1, 0);
+        if (gb_accumulate64(s->ctx, s->n, &x0, &xd, &x1, k)) return -2;
+        cols_idx(AX64, NULL, k, &x0, 0);
+        cols_idx(AXn, NULL, k, &xd, 0);
+        cols_idx(AX64n, NULL, k, &x1, 0);
+        if (++refresh >= ACC64_REFRESH) {
+          /* exact A X: the FP32 corrections of AX drift from A X */
+          refresh = 0;
+          if (d_apply(s, s->A, s->Adata, X64n, AX64n)) return -2;
+          if (gb_convert(s->ctx, s->n, GPU_MV_FLOAT64, &x1, GPU_MV_FLOAT32, &xd, k)) return -2;
+        } else if (gb_accumulate64(s->ctx, s->n, &x0, &xd, &x1, k)) {
+          return -2;
+        }
+        cols_idx(X64n, NULL, k, &x0, 0);
+        if (gb_rayleigh_quotients(s->ctx, GPU_MV_FLOAT64, s->n, &x0, &x1, k, eb->rq, s->lam))
+          return -2;
+        t64 = X64; X64 = X64n; X64n = t64;
+        t64 = AX64; AX64 = AX64n; AX64n = t64;
       }
       /* swap the double buffers */
       gpu_MultiVector* t;
@@ -875,7 +950,9 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       }
     }
     if (!undo) {
-      if (explicit_residual(s, X, AX, BX, act, nR)) return -2;
+      if (acc64 ? explicit_residual(s, X64, AX64, X64, act, nR)
+                : explicit_residual(s, X, AX, BX, act, nR))
+        return -2;
       /* A Ritz pair of the FP32 pencil that is not one of the operator
          (Gram errors ~1e-4 with TF32 products) shows as a jump of the
          largest residual: undo the step -- the previous block, its images
@@ -890,6 +967,10 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     }
     if (undo) {
       gpu_MultiVector* t;
+      if (acc64) {
+        t = X64; X64 = X64n; X64n = t;
+        t = AX64; AX64 = AX64n; AX64n = t;
+      }
       t = X; X = Xn; Xn = t;
       t = AX; AX = AXn; AXn = t;
       t = P; P = Pn; Pn = t;
@@ -932,6 +1013,13 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     } else if (s->verbosity == 1) {
       printf("Iteration %d \tbsize %d \tmaxres %22.14e\n", *it, nR, max_value(s->h_norm, k));
     }
+  }
+  /* the FP64 block goes straight to the caller's block */
+  if (acc64 && eb->Xout && !rc) {
+    gb_mv_set_mask_host(X64, NULL);
+    gb_mv_set_mask_host(eb->Xout, NULL);
+    if (d_copy(s, X64, eb->Xout)) return -2;
+    eb->wrote_x64 = 1;
   }
   /* the phase's block lives in s->X for the hand-over */
   if (X != s->X) {
@@ -1043,6 +1131,7 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
         printf("%d constraint\n\n", s.ny);
     }
 
+    int x64_done = 0; /* the FP32 phase left its FP64-accumulated X in Xu */
     for (int phase = mixed ? 0 : 1; phase < 2; phase++) {
       double tp = gb_now();
       gpu_MultiVector* Xp = Xu;
@@ -1053,7 +1142,7 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           break;
         }
         Xp = X32;
-      } else if (X32) {
+      } else if (X32 && !x64_done) {
         gb_mv_set_mask_host(X32, NULL);
         gb_mv_set_mask_host(Xu, NULL);
         if (d_copy(&s, X32, Xu)) {
@@ -1098,7 +1187,16 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           eb.BXn = gb_mv_create_like(s.X, s.dt);
           eb.BPn = gb_mv_create_like(s.X, s.dt);
         }
-        eb.G = (double*)gb_device_alloc(ctx, sizeof(double) * (8 * sq + 2 * (size_t)s.k3) + 64);
+        eb.G = (double*)gb_device_alloc(ctx, sizeof(double) * (8 * sq + 4 * (size_t)s.k3) + 64 +
+                                                 sizeof(int) * (8 + (size_t)s.k3));
+        /* FP64 accumulation blocks (used by the tensor-core path, B = I) */
+        if (ctx->opt.accum64 && s.noB && ctx->opt.tensor_cores && s.k <= 64) {
+          for (int b = 0; b < 2; b++) {
+            eb.X64[b] = gb_mv_create_like(s.X, GPU_MV_FLOAT64);
+            eb.AX64[b] = gb_mv_create_like(s.X, GPU_MV_FLOAT64);
+          }
+          eb.Xout = Xu;
+        }
         have_eb = 1;
         if (!eb.Xn || !eb.AXn || !eb.Pn || !eb.APn || !eb.G || (!s.noB && (!eb.BXn || !eb.BPn))) {
           exitflag = -2;
@@ -1112,7 +1210,9 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           eb.tmp = eb.H2 + sq;
           eb.d = eb.tmp + sq;
           eb.w = eb.d + s.k3;
-          eb.infos = (int*)(eb.w + s.k3);
+          eb.rq = eb.w + s.k3;
+          eb.infos = (int*)(eb.rq + 2 * (size_t)s.k3);
+          eb.pdrop = eb.infos + 8;
         }
       }
       if (exitflag == 0 && (phase == 1 || !mixed)) {
@@ -1166,6 +1266,11 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
         gpu_MultiVectorDestroy(eb.APn);
         gpu_MultiVectorDestroy(eb.BXn);
         gpu_MultiVectorDestroy(eb.BPn);
+        for (int b = 0; b < 2; b++) {
+          gpu_MultiVectorDestroy(eb.X64[b]);
+          gpu_MultiVectorDestroy(eb.AX64[b]);
+        }
+        if (eb.wrote_x64) x64_done = 1;
         gb_sync(ctx);
         gb_device_free(eb.G);
       }

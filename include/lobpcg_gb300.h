@@ -34,12 +34,18 @@ enum { GPU_MV_FLOAT64 = 0, GPU_MV_FLOAT32 = 1 };
 typedef struct {
   int precision;            /* LOBPCG_GPU_FP64 (default) or LOBPCG_GPU_MIXED */
   double compensated_below; /* mixed: hi+lo compensated Gram once max residual < this (1e-6) */
-  double fp64_below;        /* mixed: continue in FP64 once max residual < this (2e-6) */
+  double fp64_below;        /* mixed: continue in FP64 once max residual < this (0: only on
+                               convergence, stagnation or a failed factorisation) */
   int fp32_stall;           /* mixed: also switch after this many FP32 iterations without a
                                new minimum of the largest active residual (20) */
   int tensor_cores;         /* mixed: 1 = tcgen05 TF32 kernels, 0 = FP32 CUDA-core kernels */
   int potrf_fail_at;        /* tests: the Nth Cholesky reports INFO = 1 (0 = off) */
   int sygv_fail_at;         /* tests: the Nth Rayleigh-Ritz solve reports INFO = 1 (0 = off) */
+  double explicit_pivot_below; /* mixed FP32 phase: P is dropped when a Cholesky pivot ratio of the
+                               projected Gram matrix falls below this (1e-6: the FP32 Gram
+                               products do not resolve smaller angles) */
+  int accum64;              /* mixed, tensor-core path: carry X and A X in FP64 through the FP32
+                               phase, adding FP32 corrections (1, default) */
   int rr_method;            /* Rayleigh-Ritz solver: 0 = FP64 Householder tridiagonalisation,
                                bisection and inverse iteration (default); 1 = one-CTA FP64
                                Jacobi; 2 = FP32 Jacobi + FP64 refinement (order <= 192).
@@ -61,6 +67,7 @@ typedef struct {
   int rr_fallbacks;         /* solves that fell back to the one-CTA FP64 Jacobi */
   int rr_graded;            /* of those: pencils too graded for the tridiagonal solver */
   int explicit_undos;       /* mixed: FP32 steps undone after a residual jump */
+  int explicit_p_drops;     /* mixed: FP32 steps taken without P (not definite / unresolved) */
 } lobpcg_gpu_stats;
 
 /* per-kernel-class timing, collected with CUDA events on the context's
