@@ -157,6 +157,17 @@ SIGNATURES = {
     "gpu_OperatorParameterCount": (c_long, [c_void_p]),
     "gpu_OperatorGradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "gpu_MassGradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "gpu_ReadHypreIJ": (c_int, [ctypes.c_char_p, c_int, ctypes.POINTER(c_long), ctypes.POINTER(c_long),
+                                ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p),
+                                ctypes.POINTER(c_void_p)]),
+    "gpu_ReadMultiVector": (c_int, [ctypes.c_char_p, ctypes.POINTER(c_long), ctypes.POINTER(c_int),
+                                    ctypes.POINTER(c_void_p)]),
+    "gpu_ReadHypreParVectors": (c_int, [ctypes.c_char_p, c_int, c_int, ctypes.POINTER(c_long),
+                                        ctypes.POINTER(c_void_p)]),
+    "gpu_FreeHost": (None, [c_void_p]),
+    "gpu_CSRMatrixLoadHypreIJ": (c_void_p, [c_void_p, ctypes.c_char_p, c_int]),
+    "gpu_MultiVectorLoad": (c_void_p, [c_void_p, ctypes.c_char_p, c_int]),
+    "gpu_MultiVectorLoadHypreParVectors": (c_void_p, [c_void_p, ctypes.c_char_p, c_int, c_int, c_int]),
     "gpu_GramNoAlloc": (c_int, [c_int, c_long, c_void_p, c_long, c_int, c_void_p, c_long, c_int,
                                 c_void_p, c_int, c_void_p]),
 }

@@ -202,6 +202,31 @@ int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_Multi
                     gpu_MultiVector* Z, int mode);
 
 /* ---------------------------------------------------------------- */
+/* External problems: the reference tools' file formats                */
+/* ---------------------------------------------------------------- */
+
+/* Host readers (no GPU work).  HYPRE IJ matrix files <prefix>.00000 ...
+   (blopex_tools/matlab/matlab2hypre/matlab2hypreIJ.m: header "ilower iupper
+   jlower jupper", then 0-based "row col value" triples) into CSR arrays;
+   multivector text "n k" + values column by column (serial_Multi_VectorLoad,
+   blopex_serial_complex/multivector/multi_vector.c:668-700, real values);
+   HYPRE ParVector files <prefix>.j.i (matlab2hypreParVectors.m: row count,
+   then values) into a column-major n x k array.  Arrays are malloc'ed: free
+   them with gpu_FreeHost.  Return 0, -1 (a file does not open), -2 (bad or
+   short contents), -3 (index out of range), -4 (out of memory). */
+int gpu_ReadHypreIJ(const char* prefix, int nfiles, long* n, long* nnz, int** rowptr,
+                    int** colidx, double** vals);
+int gpu_ReadMultiVector(const char* path, long* n, int* k, double** data);
+int gpu_ReadHypreParVectors(const char* prefix, int k, int nfiles, long* n, double** data);
+void gpu_FreeHost(void* p);
+
+/* The same, uploaded: a CSR operator, or a device block of the given dtype. */
+gpu_Operator* gpu_CSRMatrixLoadHypreIJ(gpu_Context* ctx, const char* prefix, int nfiles);
+gpu_MultiVector* gpu_MultiVectorLoad(gpu_Context* ctx, const char* path, int dtype);
+gpu_MultiVector* gpu_MultiVectorLoadHypreParVectors(gpu_Context* ctx, const char* prefix, int k,
+                                                    int nfiles, int dtype);
+
+/* ---------------------------------------------------------------- */
 /* Derivatives of the computed eigenpairs (no counterpart in the      */
 /* reference)                                                          */
 /* ---------------------------------------------------------------- */
