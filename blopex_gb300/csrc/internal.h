@@ -68,6 +68,9 @@ struct gpu_Context {
   /* device buffers of the solver's internal blocks, kept across solves (all
      work is ordered on ctx->stream, so a returned buffer can be handed out
      again at once); freed by gpu_ContextTrim / gpu_ContextDestroy */
+  /* set around the FP32 phase's A R: FP32 blocks through CSR / 7-point
+     operators with FP64 coefficients and arithmetic */
+  int op_accurate;
   int pool_n;
   void* pool_ptr[GB_POOL_MAX];
   size_t pool_bytes[GB_POOL_MAX];

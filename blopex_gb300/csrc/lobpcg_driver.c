@@ -791,7 +791,10 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     }
     if (!s->noY && project_constraints(s, R)) return -2;
     if (!s->noB && d_apply(s, s->B, s->Bdata, R, BR)) return -2;
-    if (d_apply(s, s->A, s->Adata, R, AR)) return -2;
+    s->ctx->op_accurate = s->ctx->opt.fp32_accurate_op;
+    rc = d_apply(s, s->A, s->Adata, R, AR);
+    s->ctx->op_accurate = 0;
+    if (rc) return -2;
 
     /* Gram matrices of [X R P(act)] */
     {

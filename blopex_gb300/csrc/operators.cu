@@ -57,7 +57,10 @@ static const int h_st27_off[13][3] = {
 #define OP_CB 16
 
 // ---------------------------------------------------------------- CSR
-template <typename T, typename V>
+// T: block element type, V: value type, A: arithmetic (FP64 coefficients
+// and accumulation on FP32 blocks when the product must not lose the
+// cancellation of a smooth block: see gb_operator_apply)
+template <typename T, typename V, typename A = T>
 __global__ void __launch_bounds__(256) csr_kernel(long n, const int* __restrict__ rowptr,
                                                   const int* __restrict__ colidx,
                                                   const V* __restrict__ vals, blk_cols X,
@@ -67,15 +70,15 @@ __global__ void __launch_bounds__(256) csr_kernel(long n, const int* __restrict_
   if (r >= n) return;
   const int p0 = rowptr[r], p1 = rowptr[r + 1];
   for (int c0 = 0; c0 < w; c0 += OP_CB) {
-    T acc[OP_CB];
+    A acc[OP_CB];
 #pragma unroll
-    for (int b = 0; b < OP_CB; b++) acc[b] = T(0);
+    for (int b = 0; b < OP_CB; b++) acc[b] = A(0);
     for (int p = p0; p < p1; p++) {
       const int ci = colidx[p];
-      const T v = (T)vals[p];
+      const A v = (A)vals[p];
 #pragma unroll
       for (int b = 0; b < OP_CB; b++)
-        if (c0 + b < w) acc[b] = fma(v, ((const T*)X.col[c0 + b])[ci], acc[b]);
+        if (c0 + b < w) acc[b] = fma(v, (A)((const T*)X.col[c0 + b])[ci], acc[b]);
     }
 #pragma unroll
     for (int b = 0; b < OP_CB; b++)
@@ -93,11 +96,11 @@ __global__ void __launch_bounds__(256) csr_kernel(long n, const int* __restrict_
 // store); the six face coefficients are read once per cell.
 #define ST_TX 32
 #define ST_TY 8
-template <typename T>
+template <typename T, typename A = T>
 __global__ void __launch_bounds__(ST_TX* ST_TY) st7_kernel(int nx, int ny, int nz,
-                                                           const T* __restrict__ cx,
-                                                           const T* __restrict__ cy,
-                                                           const T* __restrict__ cz, T shift,
+                                                           const A* __restrict__ cx,
+                                                           const A* __restrict__ cy,
+                                                           const A* __restrict__ cz, A shift,
                                                            blk_cols X, blk_cols Y, int w)
 {
   const int tiles_x = (nx + ST_TX - 1) / ST_TX, tiles_y = (ny + ST_TY - 1) / ST_TY;
@@ -110,23 +113,23 @@ __global__ void __launch_bounds__(ST_TX* ST_TY) st7_kernel(int nx, int ny, int n
   const long plane = (long)nx * ny;
   const long c = (long)i + (long)nx * j + plane * k;
   const long jk = (long)j + (long)ny * k;
-  const T cw = cx[i + (long)(nx + 1) * jk];
-  const T ce = cx[i + 1 + (long)(nx + 1) * jk];
-  const T cs = cy[i + (long)nx * (j + (long)(ny + 1) * k)];
-  const T cn = cy[i + (long)nx * (j + 1 + (long)(ny + 1) * k)];
-  const T cb = cz[c];
-  const T ct = cz[c + plane];
-  const T dg = cw + ce + cs + cn + cb + ct + shift;
+  const A cw = cx[i + (long)(nx + 1) * jk];
+  const A ce = cx[i + 1 + (long)(nx + 1) * jk];
+  const A cs = cy[i + (long)nx * (j + (long)(ny + 1) * k)];
+  const A cn = cy[i + (long)nx * (j + 1 + (long)(ny + 1) * k)];
+  const A cb = cz[c];
+  const A ct = cz[c + plane];
+  const A dg = cw + ce + cs + cn + cb + ct + shift;
   // neighbour offsets, pointing at the cell itself (weight 0) off the grid
   const long ow = i > 0 ? -1 : 0, oe = i < nx - 1 ? 1 : 0;
   const long os = j > 0 ? -(long)nx : 0, on = j < ny - 1 ? (long)nx : 0;
   const long ob = k > 0 ? -plane : 0, ot = k < nz - 1 ? plane : 0;
-  const T ww = i > 0 ? cw : T(0), we = i < nx - 1 ? ce : T(0);
-  const T ws = j > 0 ? cs : T(0), wn = j < ny - 1 ? cn : T(0);
-  const T wb = k > 0 ? cb : T(0), wt = k < nz - 1 ? ct : T(0);
+  const A ww = i > 0 ? cw : A(0), we = i < nx - 1 ? ce : A(0);
+  const A ws = j > 0 ? cs : A(0), wn = j < ny - 1 ? cn : A(0);
+  const A wb = k > 0 ? cb : A(0), wt = k < nz - 1 ? ct : A(0);
   constexpr int U = 4;
   for (int col0 = 0; col0 < w; col0 += U) {
-    T v[U][7];
+    A v[U][7];
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const T* x = (const T*)X.col[col0 + u < w ? col0 + u : col0];
@@ -141,8 +144,8 @@ __global__ void __launch_bounds__(ST_TX* ST_TY) st7_kernel(int nx, int ny, int n
 #pragma unroll
     for (int u = 0; u < U; u++) {
       if (col0 + u < w)
-        ((T*)Y.col[col0 + u])[c] = dg * v[u][0] - ww * v[u][1] - we * v[u][2] - ws * v[u][3] -
-                                   wn * v[u][4] - wb * v[u][5] - wt * v[u][6];
+        ((T*)Y.col[col0 + u])[c] = (T)(dg * v[u][0] - ww * v[u][1] - we * v[u][2] - ws * v[u][3] -
+                                       wn * v[u][4] - wb * v[u][5] - wt * v[u][6]);
     }
   }
 }
@@ -457,6 +460,10 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
   gb_mv_fill_cols(Y, &yc, 0);
   const int f32 = X->dtype == GPU_MV_FLOAT32;
   if (f32 && ensure_f32(op)) return -1;
+  // FP32 blocks, FP64 coefficients and arithmetic (CSR, 7-point): for a
+  // smooth block |A x| << |A| |x|, and FP32 products and sums would lose the
+  // cancellation that A x consists of
+  const int acc64 = f32 && ctx->op_accurate && (op->kind == OPK_CSR || op->kind == OPK_ST7);
   const long n = op->n;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   const double es = f32 ? 4.0 : 8.0;
@@ -491,7 +498,10 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
   gb_prof_begin(ctx, &pr, cls);
   switch (op->kind) {
     case OPK_CSR:
-      if (f32)
+      if (acc64)
+        csr_kernel<float, double, double><<<blocks, 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx,
+                                                                      op->vals, xc, yc, w);
+      else if (f32)
         csr_kernel<float, float><<<blocks, 256, 0, S(ctx)>>>(n, op->rowptr, op->colidx, op->vals32,
                                                              xc, yc, w);
       else
@@ -501,7 +511,11 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
     case OPK_ST7: {
       const unsigned tb = (unsigned)(((op->nx + ST_TX - 1) / ST_TX) * ((op->ny + ST_TY - 1) / ST_TY) *
                                      (long)op->nz);
-      if (f32)
+      if (acc64)
+        st7_kernel<float, double><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0],
+                                                                    op->c[1], op->c[2], op->shift,
+                                                                    xc, yc, w);
+      else if (f32)
         st7_kernel<float><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0],
                                                             op->c32[1], op->c32[2], (float)op->shift,
                                                             xc, yc, w);

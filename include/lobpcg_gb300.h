@@ -44,6 +44,8 @@ typedef struct {
   double explicit_pivot_below; /* mixed FP32 phase: P is dropped when a Cholesky pivot ratio of the
                                projected Gram matrix falls below this (1e-6: the FP32 Gram
                                products do not resolve smaller angles) */
+  int fp32_accurate_op;      /* mixed FP32 phase: apply A to the residual block with FP64
+                               coefficients and arithmetic (CSR and 7-point operators; 0) */
   int accum64;              /* mixed, tensor-core path: carry X and A X in FP64 through the FP32
                                phase, adding FP32 corrections (1, default) */
   int rr_method;            /* Rayleigh-Ritz solver: 0 = FP64 Householder tridiagonalisation,
