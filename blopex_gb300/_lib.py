@@ -28,7 +28,9 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("compensated_below", c_double), ("fp64_below", c_double),
                 ("fp32_stall", c_int), ("tensor_cores", c_int), ("potrf_fail_at", c_int),
                 ("sygv_fail_at", c_int), ("explicit_pivot_below", c_double),
-                ("fp32_accurate_op", c_int), ("accum64", c_int), ("rr_method", c_int)]
+                ("fp32_accurate_op", c_int), ("recompute_ap", c_int), ("explicit_fp64", c_int),
+                ("accum64", c_int),
+                ("rr_method", c_int)]
 
 
 class Stats(ctypes.Structure):

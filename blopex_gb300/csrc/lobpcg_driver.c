@@ -746,7 +746,12 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         ctl->handed_over = 1;
         break;
       }
-      if (tc_ok && !comp && mx < s->ctx->opt.compensated_below) {
+      /* TF32 products carry ~1e-4 relative errors: compensate once the
+         residuals approach that fraction of the Ritz values' scale (or the
+         absolute threshold, whichever is reached first) */
+      double lmax = 0.0;
+      for (int i = 0; i < k; i++) lmax = fmax(lmax, fabs(s->h_lam[i]));
+      if (tc_ok && !comp && (mx < s->ctx->opt.compensated_below || mx < 1e-3 * lmax)) {
         comp = 1;
         stall = 0;
       }
@@ -888,7 +893,18 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         cols_idx(srcs[q][2], NULL, k, &y, 0);
         cols_idx(xs[q][0], NULL, k, &xa, 0);
         cols_idx(xs[q][1], NULL, k, &z, 0);
-        if (tc_ok) {
+        if (q == 1 && s->ctx->opt.recompute_ap) {
+          /* A P from P itself: the update [AR AP] C_RP rounds with the
+             cancellation between the R and P coefficients (large when R and
+             P are nearly dependent), and an A P that drifts from A times P
+             corrupts the next pencil in FP32 */
+          gb_mv_set_mask_host(Pn, NULL);
+          gb_mv_set_mask_host(APn, NULL);
+          if (d_apply(s, s->A, s->Adata, Pn, APn)) return -2;
+          if (tc_ok ? gb_tc_xc(s->ctx, s->n, &xa, k, cX, k3, &z, k, &y)
+                    : gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y))
+            return -2;
+        } else if (tc_ok) {
           if (gb_tc_xc(s->ctx, s->n, &a, h, cRP, k3, &y, k, NULL)) return -2;
           if (gb_tc_xc(s->ctx, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
         } else {
@@ -1139,7 +1155,7 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
       double tp = gb_now();
       gpu_MultiVector* Xp = Xu;
       if (phase == 0) {
-        X32 = gb_mv_create_like(Xu, GPU_MV_FLOAT32);
+        X32 = gb_mv_create_like(Xu, ctx->opt.explicit_fp64 ? GPU_MV_FLOAT64 : GPU_MV_FLOAT32);
         if (!X32 || d_copy(&s, Xu, X32)) {
           exitflag = -2;
           break;

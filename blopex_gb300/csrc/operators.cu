@@ -954,19 +954,27 @@ static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
   }
   if (gb_axpby(ctx, dt, op->n, 1.0, &cz, 0.0, &cp, w)) return -1;
   if (gb_dot_cols(ctx, dt, op->n, &cr, &cz, w, rho, idx)) return -1;
+  // FP32 blocks: the inner products A p with FP64 coefficients and
+  // arithmetic when the context asks for accurate FP32 operators
+  const int acc_saved = ctx->op_accurate;
+  if (f32 && ctx->opt.fp32_accurate_op) ctx->op_accurate = 1;
   for (int it = 0; it < op->iters; it++) {
-    if (gb_operator_apply(op->inner, p, q)) return -1;
-    if (gb_dot_cols(ctx, dt, op->n, &cp, &cq, w, pq, idx)) return -1;
+    const int rca = gb_operator_apply(op->inner, p, q);
+    if (rca) {
+      ctx->op_accurate = acc_saved;
+      { ctx->op_accurate = acc_saved; return -1; }
+    }
+    if (gb_dot_cols(ctx, dt, op->n, &cp, &cq, w, pq, idx)) { ctx->op_accurate = acc_saved; return -1; }
     pcg_ratio_kernel<<<1, BLK_MAXCOLS, 0, S(ctx)>>>(w, rho, pq, al);
     gb_count_launch(1);
     PCG_COLS(it == 0 ? 0 : 1, cp, cq, cy, cr, al);  // y += alpha p ; r -= alpha q
     if (it + 1 == op->iters) break;
     if (op->prec) {
-      if (gb_operator_apply(op->prec, r, z)) return -1;
+      if (gb_operator_apply(op->prec, r, z)) { ctx->op_accurate = acc_saved; return -1; }
     } else if (gb_axpby(ctx, dt, op->n, 1.0, &cr, 0.0, &cz, w)) {
-      return -1;
+      { ctx->op_accurate = acc_saved; return -1; }
     }
-    if (gb_dot_cols(ctx, dt, op->n, &cr, &cz, w, rho2, idx)) return -1;
+    if (gb_dot_cols(ctx, dt, op->n, &cr, &cz, w, rho2, idx)) { ctx->op_accurate = acc_saved; return -1; }
     pcg_ratio_kernel<<<1, BLK_MAXCOLS, 0, S(ctx)>>>(w, rho2, rho, al);  // beta
     gb_count_launch(1);
     PCG_COLS(2, cz, cz, cp, cp, al);  // p = z + beta p
@@ -975,5 +983,6 @@ static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
     rho2 = t;
   }
 #undef PCG_COLS
+  ctx->op_accurate = acc_saved;
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "pcg preconditioner");
 }

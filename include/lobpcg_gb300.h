@@ -46,6 +46,10 @@ typedef struct {
                                products do not resolve smaller angles) */
   int fp32_accurate_op;      /* mixed FP32 phase: apply A to the residual block with FP64
                                coefficients and arithmetic (CSR and 7-point operators; 0) */
+  int recompute_ap;          /* mixed FP32 phase: A P applied to the new P instead of updated
+                               from [AR AP] (1) */
+  int explicit_fp64;        /* diagnostics: run the mixed mode's explicit-Gram phase on FP64
+                               blocks (CUDA-core kernels), to separate algorithm from precision */
   int accum64;              /* mixed, tensor-core path: carry X and A X in FP64 through the FP32
                                phase, adding FP32 corrections (1, default) */
   int rr_method;            /* Rayleigh-Ritz solver: 0 = FP64 Householder tridiagonalisation,
