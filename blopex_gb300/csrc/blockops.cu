@@ -130,7 +130,7 @@ static int gram_launch(gpu_Context* ctx, long n, const blk_cols* X, int h, const
   if (!partial) return -1;
   dim3 grid(gx, gy, (unsigned)splits);
   gb_prof_rec pr;
-  gb_prof_begin(ctx, &pr, GB_K_GRAM);
+  gb_prof_begin(ctx, &pr, sizeof(T) == 8 ? GB_K_GRAM : GB_K_GRAM32);
   gram_partial_kernel<T, TM, TN><<<grid, 256, 0, S(ctx)>>>(*X, h, *Y, w, n, rows, partial);
   int tot = h * w;
   gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, S(ctx)>>>(partial, (int)splits, h, w, G, ldg);
@@ -217,7 +217,7 @@ extern "C" int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, 
   const blk_cols* z = Z ? Z : &empty;
   const double es = dtype == GPU_MV_FLOAT64 ? 8.0 : 4.0;
   gb_prof_rec pr;
-  gb_prof_begin(ctx, &pr, GB_K_XC);
+  gb_prof_begin(ctx, &pr, dtype == GPU_MV_FLOAT64 ? GB_K_XC : GB_K_XC32);
   if (dtype == GPU_MV_FLOAT64)
     bymat_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n);
   else

@@ -27,7 +27,10 @@ enum {
   GB_K_GRAM = 0, GB_K_XC, GB_K_CSR, GB_K_ST7, GB_K_ST5, GB_K_ST27, GB_K_DIAG, GB_K_RESID,
   GB_K_BLAS1, GB_K_CHOLQR, GB_K_SYGV, GB_K_SMALL, GB_K_TC_GRAM, GB_K_TC_XC, GB_K_SYGV_FALLBACK,
   GB_K_RR_CHOL, GB_K_RR_TRSM, GB_K_RR_JAC32, GB_K_RR_GEMM, GB_K_RR_REFINE, GB_K_RR_TRID,
-  GB_K_RR_EIG, GB_K_COUNT
+  GB_K_RR_EIG,
+  /* the same operations with FP32 arithmetic (the mixed mode's FP32 phase) */
+  GB_K_GRAM32, GB_K_XC32, GB_K_CSR32, GB_K_ST7_32, GB_K_ST5_32, GB_K_ST27_32, GB_K_DIAG32,
+  GB_K_COUNT
 };
 
 typedef struct {

@@ -11,6 +11,7 @@
 // operator to up to 16 columns at once so the coefficients are read once per
 // 16 columns; the x gathers of a warp are coalesced along the row index.
 #include <cuda_runtime.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -147,6 +148,161 @@ __global__ void __launch_bounds__(ST_TX* ST_TY) st7_kernel(int nx, int ny, int n
         ((T*)Y.col[col0 + u])[c] = (T)(dg * v[u][0] - ww * v[u][1] - we * v[u][2] - ws * v[u][3] -
                                        wn * v[u][4] - wb * v[u][5] - wt * v[u][6]);
     }
+  }
+}
+
+// ------------------------------------------------- 7-point, FP32 column ring
+// FP32 blocks, nx a multiple of 4, 16-byte-aligned input columns.  A CTA owns
+// a 32 x 32 tile of one plane (each thread four cells stacked in y) and
+// walks the block columns.  Per column it needs the tile with a one-cell
+// halo in x and y (34 rows of 40 floats, cells at offsets 4-35) and the tiles
+// of the planes below and above: 3408 floats, copied as 784 16-byte pieces
+// and 68 4-byte x-halo cells with cp.async (the plan, up to four copies per
+// thread, is the same for every column) into a ring of ST7R_DEPTH slots,
+// ST7R_DEPTH - 1 columns ahead of the column being computed.  The bytes in
+// flight occupy shared memory instead of registers, loads of X never wait
+// behind stores of Y, and the y neighbours of a thread's cells come from its
+// own registers.  Neighbours off the grid are zero-filled (src-size 0) and
+// carry zero weights.  No spin-waits: the ring is ordered by
+// cp.async.wait_group and one barrier per column.
+#define ST7R_DEPTH 3
+#define ST7R_ROW 40
+#define ST7R_BELOW (34 * ST7R_ROW)
+#define ST7R_ABOVE (ST7R_BELOW + 1024)
+#define ST7R_SLOT (ST7R_ABOVE + 1024)
+#define ST7R_PIECES 784  // 16-byte pieces per column
+#define ST7R_COPIES 852  // + 68 halo cells
+
+static __device__ __forceinline__ void st7r_copy(uint32_t dst, const float* src, int e, int nbytes)
+{
+  if (e < ST7R_PIECES)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(nbytes)
+                 : "memory");
+  else if (e < ST7R_COPIES)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(nbytes)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(256) st7_ring_kernel(int nx, int ny, int nz,
+                                                       const float* __restrict__ cx,
+                                                       const float* __restrict__ cy,
+                                                       const float* __restrict__ cz, float shift,
+                                                       const __grid_constant__ blk_cols X,
+                                                       const __grid_constant__ blk_cols Y, int w)
+{
+  __shared__ __align__(16) float ring[ST7R_DEPTH * ST7R_SLOT];
+  const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
+  const int tiles_x = (nx + 31) / 32, tiles_y = (ny + 31) / 32;
+  const long b = blockIdx.x;
+  const int tile = (int)(b % ((long)tiles_x * tiles_y));
+  const int k = (int)(b / ((long)tiles_x * tiles_y));
+  const int i0 = (tile % tiles_x) * 32, j0 = (tile / tiles_x) * 32;
+  const long plane = (long)nx * ny;
+
+  // copy plan: copy e = t + 256 q; source offset from the column base (the
+  // columns hold fewer than 2^31 elements), destination float in the slot,
+  // byte count (0 = zero fill)
+  int src[4], dst[4], nb[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int e = t + 256 * q;
+    bool ok = false;
+    long so = 0;
+    int d = 0;
+    if (e < 272) {  // centre plane, rows j0-1 .. j0+32, eight pieces each
+      const int row = e >> 3, x = i0 + 4 * (e & 7), y = j0 - 1 + row;
+      ok = y >= 0 && y < ny && x < nx;
+      d = row * ST7R_ROW + 4 + 4 * (e & 7);
+      so = (long)x + (long)nx * y + plane * k;
+    } else if (e < ST7R_PIECES) {  // planes k-1 and k+1, rows j0 .. j0+31
+      const int u = e - 272, above = u >> 8, r = (u >> 3) & 31, x = i0 + 4 * (u & 7), y = j0 + r;
+      const int z = above ? k + 1 : k - 1;
+      ok = y < ny && x < nx && z >= 0 && z < nz;
+      d = (above ? ST7R_ABOVE : ST7R_BELOW) + r * 32 + 4 * (u & 7);
+      so = (long)x + (long)nx * y + plane * z;
+    } else if (e < ST7R_COPIES) {  // x halo: cells i0-1 and i0+32 of the 34 centre rows
+      const int u = e - ST7R_PIECES, row = u >> 1, east = u & 1;
+      const int x = east ? i0 + 32 : i0 - 1, y = j0 - 1 + row;
+      ok = y >= 0 && y < ny && x >= 0 && x < nx;
+      d = row * ST7R_ROW + (east ? 36 : 3);
+      so = (long)x + (long)nx * y + plane * k;
+    }
+    src[q] = ok ? (int)so : 0;
+    dst[q] = d;
+    nb[q] = ok ? (e < ST7R_PIECES ? 16 : 4) : 0;
+  }
+  const uint32_t ring_s = (uint32_t)__cvta_generic_to_shared(ring);
+
+#pragma unroll 1
+  for (int c = 0; c < ST7R_DEPTH - 1; c++) {
+    if (c < w) {
+      const float* base = (const float*)X.col[c];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        st7r_copy(ring_s + 4u * (ST7R_SLOT * c + dst[q]), base + src[q], t + 256 * q, nb[q]);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+
+  // coefficients of the thread's four cells (rows j0 + 4 ty .. + 3)
+  const int i = i0 + tx, jb = j0 + 4 * ty;
+  float dg[4], ww[4], we[4], ws[4], wn[4], wb[4], wt[4];
+  bool valid[4];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const int j = jb + s;
+    valid[s] = i < nx && j < ny;
+    dg[s] = ww[s] = we[s] = ws[s] = wn[s] = wb[s] = wt[s] = 0.f;
+    if (valid[s]) {
+      const long cell = (long)i + (long)nx * j + plane * k;
+      const long jk = (long)j + (long)ny * k;
+      const float cw = cx[i + (long)(nx + 1) * jk];
+      const float ce = cx[i + 1 + (long)(nx + 1) * jk];
+      const float cs = cy[i + (long)nx * (j + (long)(ny + 1) * k)];
+      const float cn = cy[i + (long)nx * (j + 1 + (long)(ny + 1) * k)];
+      const float cb = cz[cell];
+      const float ct = cz[cell + plane];
+      dg[s] = cw + ce + cs + cn + cb + ct + shift;
+      ww[s] = i > 0 ? cw : 0.f;
+      we[s] = i < nx - 1 ? ce : 0.f;
+      ws[s] = j > 0 ? cs : 0.f;
+      wn[s] = j < ny - 1 ? cn : 0.f;
+      wb[s] = k > 0 ? cb : 0.f;
+      wt[s] = k < nz - 1 ? ct : 0.f;
+    }
+  }
+  const long cell0 = (long)i + (long)nx * jb + plane * k;
+
+  int slot = 0, ahead_slot = ST7R_DEPTH - 1;
+#pragma unroll 1
+  for (int col = 0; col < w; col++) {
+    asm volatile("cp.async.wait_group %0;" ::"n"(ST7R_DEPTH - 2) : "memory");
+    __syncthreads();  // column col landed for all threads; the slot of col - 1 is free
+    const int ahead = col + ST7R_DEPTH - 1;
+    if (ahead < w) {
+      const float* base = (const float*)X.col[ahead];
+      const uint32_t so = ring_s + 4u * ST7R_SLOT * ahead_slot;
+#pragma unroll
+      for (int q = 0; q < 4; q++) st7r_copy(so + 4u * dst[q], base + src[q], t + 256 * q, nb[q]);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    const float* sl = ring + ST7R_SLOT * slot;
+    float cv[6];
+#pragma unroll
+    for (int r = 0; r < 6; r++) cv[r] = sl[(4 * ty + r) * ST7R_ROW + 4 + tx];
+    float* y = (float*)Y.col[col] + cell0;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const int m = (4 * ty + 1 + s) * ST7R_ROW + 4 + tx;
+      const float v1 = sl[m - 1], v2 = sl[m + 1];
+      const float v5 = sl[ST7R_BELOW + (4 * ty + s) * 32 + tx];
+      const float v6 = sl[ST7R_ABOVE + (4 * ty + s) * 32 + tx];
+      if (valid[s])
+        __stcs(y + (long)nx * s, dg[s] * cv[s + 1] - ww[s] * v1 - we[s] * v2 - ws[s] * cv[s] -
+                                     wn[s] * cv[s + 2] - wb[s] * v5 - wt[s] * v6);
+    }
+    slot = slot == ST7R_DEPTH - 1 ? 0 : slot + 1;
+    ahead_slot = ahead_slot == ST7R_DEPTH - 1 ? 0 : ahead_slot + 1;
   }
 }
 
@@ -438,6 +594,16 @@ static int ensure_f32(gpu_Operator* op)
   return 0;
 }
 
+// the ring kernel copies 16-byte pieces (rows of whole 16-byte groups, input
+// columns on 16-byte boundaries) and addresses a column with 32-bit offsets
+static int st7_ring_ok(const gpu_Operator* op, const blk_cols* xc, int w)
+{
+  if (op->nx % 4 || op->n >= (1L << 31)) return 0;
+  for (int c = 0; c < w; c++)
+    if ((uintptr_t)xc->col[c] & 15) return 0;
+  return 1;
+}
+
 static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
 
 extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
@@ -494,6 +660,15 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
       bytes += es * n;
       flops = 1.0 * n * w;
   }
+  if (f32 && !acc64) {  // FP32 arithmetic: timed apart from the FP64 launches
+    switch (cls) {
+      case GB_K_CSR: cls = GB_K_CSR32; break;
+      case GB_K_ST7: cls = GB_K_ST7_32; break;
+      case GB_K_ST5: cls = GB_K_ST5_32; break;
+      case GB_K_ST27: cls = GB_K_ST27_32; break;
+      default: cls = GB_K_DIAG32;
+    }
+  }
   gb_prof_rec pr;
   gb_prof_begin(ctx, &pr, cls);
   switch (op->kind) {
@@ -515,6 +690,10 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
         st7_kernel<float, double><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0],
                                                                     op->c[1], op->c[2], op->shift,
                                                                     xc, yc, w);
+      else if (f32 && st7_ring_ok(op, &xc, w))
+        st7_ring_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
+                          0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
+                                                op->c32[2], (float)op->shift, xc, yc, w);
       else if (f32)
         st7_kernel<float><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0],
                                                             op->c32[1], op->c32[2], (float)op->shift,

@@ -80,8 +80,8 @@ class Context:
 
     def kernel_times(self) -> dict:
         """{class: {launches, ms, bytes, flops}} from the CUDA-event timers."""
-        buf = (_lib.KernelTime * 32)()
-        n = self.lib.gpu_ContextKernelTimes(self.handle, buf, 32)
+        buf = (_lib.KernelTime * 64)()
+        n = self.lib.gpu_ContextKernelTimes(self.handle, buf, 64)
         return {buf[i].name.decode(): {"launches": buf[i].launches, "ms": buf[i].ms,
                                        "bytes": buf[i].bytes, "flops": buf[i].flops}
                 for i in range(n)}

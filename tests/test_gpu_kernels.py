@@ -79,6 +79,11 @@ def _ops(ctx):
     # several (x, y) tiles and z chunks of the blocked kernel, ragged edges
     cx, cy, cz = P.stencil7_coefficients(37, 9, 70, seed=5)
     out.append((S.Stencil7(ctx, cx, cy, cz, 0.0), O.stencil7(37, 9, 70, cx, cy, cz, 0.0), 23310))
+    # nx a multiple of 4: the FP32 column-ring kernel (ragged and whole tiles)
+    cx, cy, cz = P.stencil7_coefficients(44, 10, 6, seed=8)
+    out.append((S.Stencil7(ctx, cx, cy, cz, 0.2), O.stencil7(44, 10, 6, cx, cy, cz, 0.2), 2640))
+    cx, cy, cz = P.stencil7_coefficients(64, 40, 3, seed=9)
+    out.append((S.Stencil7(ctx, cx, cy, cz, 0.0), O.stencil7(64, 40, 3, cx, cy, cz, 0.0), 7680))
     c = np.exp(rng.standard_normal((13, 17)))
     sx, sy = P.stencil5_from_cells(c)
     out.append((S.Stencil5(ctx, sx, sy, 0.1), O.stencil5(17, 13, sx, sy, 0.1), 221))
