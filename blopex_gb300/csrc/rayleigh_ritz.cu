@@ -133,66 +133,82 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
   }
 }
 
-// triangular solves with the FP64 factor, one warp per right-hand side; the
-// solution lives in registers (entry p in lane p % 32, slot p / 32):
+// triangular solves with the FP64 factor, one warp (one CTA) per right-hand
+// side, column-oriented like the reference BLAS dtrsm: once x_i is known it
+// is broadcast from its lane and subtracted from the entries still to be
+// solved, so no step needs a reduction across the warp.  The right-hand side
+// lives in registers (entry p in lane p % 32, slot p / 32; SL = ceil(m / 32)
+// slots):
 //   mode 0: X = inv(L) Y, Y symmetric read from its lower triangle (ld ldy)
 //   mode 1: X = inv(L) Y' (Y m x m, ld ldy)
 //   mode 2: X = inv(L)' Y (Y m x m, ld ldy), result to X with leading dim ldx
-// s.LT holds L row-major (LT[p + i*m] = L(i, p)) so that the forward
-// sweeps read contiguous rows of L.
+// The forward sweeps read columns of L (s.L64), the backward sweep columns
+// of L' = rows of L (s.LT64, LT[p + i*m] = L(i, p)): contiguous either way.
 #define RR_TRSM_SLOTS (RR_MAX_M / 32)
-__global__ void __launch_bounds__(256) rr_trsm64_kernel(int mode, const double* __restrict__ Y,
-                                                        int ldy, double* __restrict__ X, int ldx,
-                                                        int m, int ncols, rr_scratch s)
+template <int SL>
+__global__ void __launch_bounds__(32) rr_trsm64_kernel(int mode, const double* __restrict__ Y,
+                                                       int ldy, double* __restrict__ X, int ldx,
+                                                       int m, int ncols, rr_scratch s)
 {
   if (s.status[0]) return;
-  const int lane = threadIdx.x & 31;
-  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x;
+  const int j = blockIdx.x;
   if (j >= ncols) return;
-  double xr[RR_TRSM_SLOTS];
+  double y[SL];
 #pragma unroll
-  for (int q = 0; q < RR_TRSM_SLOTS; q++) xr[q] = 0.0;
-  if (mode < 2) {
-    const double* LT = s.LT64;
-    for (int i = 0; i < m; i++) {
-      double part = 0.0;
-#pragma unroll
-      for (int q = 0; q < RR_TRSM_SLOTS; q++) {
-        int p = q * 32 + lane;
-        if (p < i) part += LT[p + (size_t)i * m] * xr[q];
-      }
-      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-      double a;
+  for (int q = 0; q < SL; q++) {
+    const int p = q * 32 + lane;
+    double a = 0.0;
+    if (p < m) {
       if (mode == 0)
-        a = (i >= j) ? Y[i + (size_t)j * ldy] : Y[j + (size_t)i * ldy];
+        a = (p >= j) ? Y[p + (size_t)j * ldy] : Y[j + (size_t)p * ldy];
+      else if (mode == 1)
+        a = Y[j + (size_t)p * ldy];
       else
-        a = Y[j + (size_t)i * ldy];
-      const double xi = (a - part) / LT[i + (size_t)i * m];
+        a = Y[p + (size_t)j * ldy];
+    }
+    y[q] = a;
+  }
+  if (mode < 2) {
+    const double* L = s.L64;
 #pragma unroll
-      for (int q = 0; q < RR_TRSM_SLOTS; q++)
-        if (q * 32 + lane == i) xr[q] = xi;
+    for (int q = 0; q < SL; q++) {
+      for (int il = 0; il < 32; il++) {
+        const int i = q * 32 + il;
+        if (i >= m) break;
+        const double* li = L + (size_t)i * m;
+        const double xi = __shfl_sync(0xffffffffu, y[q], il) / li[i];
+        if (lane == il) y[q] = xi;
+#pragma unroll
+        for (int q2 = q; q2 < SL; q2++) {
+          const int p = q2 * 32 + lane;
+          if (p > i && p < m) y[q2] -= li[p] * xi;
+        }
+      }
     }
   } else {
-    const double* L = s.L64;
-    for (int i = m - 1; i >= 0; i--) {
-      double part = 0.0;
+    const double* LT = s.LT64;
 #pragma unroll
-      for (int q = 0; q < RR_TRSM_SLOTS; q++) {
-        int p = q * 32 + lane;
-        if (p > i && p < m) part += L[p + (size_t)i * m] * xr[q];
+    for (int q = SL - 1; q >= 0; q--) {
+      for (int il = 31; il >= 0; il--) {
+        const int i = q * 32 + il;
+        if (i >= m) continue;
+        const double* lti = LT + (size_t)i * m;  // lti[p] = L(i, p)
+        const double xi = __shfl_sync(0xffffffffu, y[q], il) / lti[i];
+        if (lane == il) y[q] = xi;
+#pragma unroll
+        for (int q2 = 0; q2 <= q; q2++) {
+          const int p = q2 * 32 + lane;
+          if (p < i) y[q2] -= lti[p] * xi;
+        }
       }
-      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-      const double xi = (Y[i + (size_t)j * ldy] - part) / L[i + (size_t)i * m];
-#pragma unroll
-      for (int q = 0; q < RR_TRSM_SLOTS; q++)
-        if (q * 32 + lane == i) xr[q] = xi;
     }
   }
   double* x = X + (size_t)j * ldx;
 #pragma unroll
-  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
-    int p = q * 32 + lane;
-    if (p < m) x[p] = xr[q];
+  for (int q = 0; q < SL; q++) {
+    const int p = q * 32 + lane;
+    if (p < m) x[p] = y[q];
   }
 }
 
@@ -1051,17 +1067,19 @@ __global__ void __launch_bounds__(256) rr_cholinv_kernel(int nev, rr_scratch s)
   }
 }
 
-// 6. z <- H_0 H_1 ... H_{m-3} z for the nev vectors of s.X, one warp per vector
-__global__ void __launch_bounds__(256) rr_backtr_kernel(int m, int nev, rr_scratch s)
+// 6. z <- H_0 H_1 ... H_{m-3} z for the nev vectors of s.X, one warp (one
+// CTA) per vector, SL = ceil(m / 32) register slots
+template <int SL>
+__global__ void __launch_bounds__(32) rr_backtr_kernel(int m, int nev, rr_scratch s)
 {
   if (s.status[0]) return;
-  const int lane = threadIdx.x & 31;
-  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x;
+  const int j = blockIdx.x;
   if (j >= nev) return;
-  double z[RR_TRSM_SLOTS];
+  double z[SL];
   double* zc = s.X + (size_t)j * m;
 #pragma unroll
-  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+  for (int q = 0; q < SL; q++) {
     const int i = q * 32 + lane;
     z[q] = i < m ? zc[i] : 0.0;
   }
@@ -1071,7 +1089,7 @@ __global__ void __launch_bounds__(256) rr_backtr_kernel(int m, int nev, rr_scrat
     const double* vh = s.C64 + (size_t)h * m;  // v(h+1) = 1, v(i) = C[i, h] for i >= h+2
     double t = 0.0;
 #pragma unroll
-    for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+    for (int q = 0; q < SL; q++) {
       const int i = q * 32 + lane;
       if (i == h + 1)
         t += z[q];
@@ -1080,7 +1098,7 @@ __global__ void __launch_bounds__(256) rr_backtr_kernel(int m, int nev, rr_scrat
     }
     t = tau * rr_warp_sum(t);
 #pragma unroll
-    for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+    for (int q = 0; q < SL; q++) {
       const int i = q * 32 + lane;
       if (i == h + 1)
         z[q] -= t;
@@ -1089,11 +1107,36 @@ __global__ void __launch_bounds__(256) rr_backtr_kernel(int m, int nev, rr_scrat
     }
   }
 #pragma unroll
-  for (int q = 0; q < RR_TRSM_SLOTS; q++) {
+  for (int q = 0; q < SL; q++) {
     const int i = q * 32 + lane;
     if (i < m) zc[i] = z[q];
   }
 }
+
+// launch with the register slots m needs (m <= RR_MAX_M)
+#define RR_SL_CASES(F) \
+  F(1) F(2) F(3) F(4) F(5) F(6) F(7) F(8) F(9) F(10) F(11) F(12)
+static void rr_trsm(cudaStream_t st, int mode, const double* Y, int ldy, double* X, int ldx, int m,
+                    int ncols, const rr_scratch& s)
+{
+  switch ((m + 31) / 32) {
+#define RR_TRSM_CASE(n) \
+  case n: rr_trsm64_kernel<n><<<ncols, 32, 0, st>>>(mode, Y, ldy, X, ldx, m, ncols, s); break;
+    RR_SL_CASES(RR_TRSM_CASE)
+#undef RR_TRSM_CASE
+  }
+}
+
+static void rr_backtr(cudaStream_t st, int m, int nev, const rr_scratch& s)
+{
+  switch ((m + 31) / 32) {
+#define RR_BACKTR_CASE(n) \
+  case n: rr_backtr_kernel<n><<<nev, 32, 0, st>>>(m, nev, s); break;
+    RR_SL_CASES(RR_BACKTR_CASE)
+#undef RR_BACKTR_CASE
+  }
+}
+static_assert(RR_MAX_M <= 12 * 32, "rr_trsm / rr_backtr cases cover m <= 384");
 
 // gated FP64 fallback (dense.cu)
 extern "C" int gb_sygv_fp64(gpu_Context* ctx, double* A, double* B, int ld, int m, double* w,
@@ -1142,10 +1185,9 @@ static void rr_reduce(gpu_Context* ctx, double* A, double* B, int ld, int m, int
   gb_prof_rec ps;
   const double m3 = (double)m * m * m;
   const size_t mm = (size_t)m * m;
-  const unsigned tb = (unsigned)((m + 7) / 8);  // 8 warps (columns) per CTA
   RR_STAGE(GB_K_RR_CHOL, m3 / 3, (rr_chol64_kernel<<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info, report_below)));
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(0, A, ld, s.W64, m, m, m, s)));
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(1, s.W64, m, s.C64, m, m, m, s)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm(st, 0, A, ld, s.W64, m, m, m, s)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm(st, 1, s.W64, m, s.C64, m, m, m, s)));
   if (jacobi32) rr_sym_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
   rr_sym_store_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
   gb_count_launch(4 + jacobi32);
@@ -1179,10 +1221,9 @@ static void rr_tridiag_path(gpu_Context* ctx, double* A, int ld, int m, int nev,
     s.X = s.Xn;
     s.Xn = t;
   }
-  const unsigned tv = (unsigned)((nev + 7) / 8);
-  RR_STAGE(GB_K_RR_TRSM, 2.0 * m * m * nev, (rr_backtr_kernel<<<tv, 256, 0, st>>>(m, nev, s)));
+  RR_STAGE(GB_K_RR_TRSM, 2.0 * m * m * nev, (rr_backtr(st, m, nev, s)));
   RR_STAGE(GB_K_RR_TRSM, (double)m * m * nev,
-           (rr_trsm64_kernel<<<tv, 256, 0, st>>>(2, s.X, m, A, ld, m, nev, s)));
+           (rr_trsm(st, 2, s.X, m, A, ld, m, nev, s)));
   rr_finish_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(nev, s, w, info);
   gb_count_launch(12);
 }
@@ -1221,8 +1262,7 @@ static void rr_jacobi32_path(gpu_Context* ctx, double* A, int ld, int m, int nev
     launches += 5;
   }
   // eigenvectors of the pencil: inv(L)' X into A; values into w
-  const unsigned tb = (unsigned)((m + 7) / 8);
-  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm64_kernel<<<tb, 256, 0, st>>>(2, s.X, m, A, ld, m, m, s)));
+  RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm(st, 2, s.X, m, A, ld, m, m, s)));
   rr_finish_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(nev, s, w, info);
   gb_count_launch(launches + 2);
 }
