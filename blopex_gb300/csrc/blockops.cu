@@ -10,6 +10,7 @@
 // deterministic run to run.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "internal.h"
 
@@ -110,6 +111,134 @@ __global__ void gram_reduce_kernel(const double* __restrict__ partial, int split
   G[(size_t)j * ldg + i] = s;
 }
 
+// Symmetric Gram X'X (h <= 64) on the lower triangle only.  Thread t owns
+// the BS x BS block (bi, bj), bi >= bj, of the triangular numbering t =
+// bi (bi + 1) / 2 + bj, so whole warps drop out of the upper triangle (a
+// warp-wide FP64 instruction costs the same whatever its lane count).  Row
+// splits, staging, the order of the multiply-adds into each entry and the
+// flushes to FP64 are those of gram_partial_kernel, so every entry (and its
+// mirror, as x_i x_j = x_j x_i exactly) is bit-identical to the full
+// product's.
+template <typename T, int BS>
+__global__ void __launch_bounds__(544) gram_sym_partial_kernel(blk_cols X, int h, long n,
+                                                               long rows_per_split,
+                                                               double* __restrict__ partial)
+{
+  constexpr int BM = 32 * BS, RK = 32;
+  __shared__ T xs[RK][BM + 1];
+  const int t = threadIdx.x;
+  const int nb = (h + BS - 1) / BS;
+  const bool active = t < nb * (nb + 1) / 2;
+  int bi = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while (bi * (bi + 1) / 2 > t) bi--;
+  while ((bi + 1) * (bi + 2) / 2 <= t) bi++;
+  const int bj = t - bi * (bi + 1) / 2;
+  const long r_begin = (long)blockIdx.z * rows_per_split;
+  const long r_end = min(n, r_begin + rows_per_split);
+
+  double acc[BS][BS];
+  T accs[BS][BS];
+#pragma unroll
+  for (int a = 0; a < BS; a++)
+#pragma unroll
+    for (int b = 0; b < BS; b++) {
+      acc[a][b] = 0.0;
+      accs[a][b] = T(0);
+    }
+
+  int chunk = 0;
+  for (long r0 = r_begin; r0 < r_end; r0 += RK) {
+    for (int e = t; e < RK * BM; e += blockDim.x) {
+      int rr = e % RK, cc = e / RK;
+      long r = r0 + rr;
+      T v = T(0);
+      if (r < r_end && cc < h) v = ((const T*)X.col[cc])[r];
+      xs[rr][cc] = v;
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll 8
+      for (int rr = 0; rr < RK; rr++) {
+        T xv[BS], yv[BS];
+#pragma unroll
+        for (int a = 0; a < BS; a++) xv[a] = xs[rr][BS * bi + a];
+#pragma unroll
+        for (int b = 0; b < BS; b++) yv[b] = xs[rr][BS * bj + b];
+#pragma unroll
+        for (int a = 0; a < BS; a++)
+#pragma unroll
+          for (int b = 0; b < BS; b++) accs[a][b] = fma(xv[a], yv[b], accs[a][b]);
+      }
+    }
+    __syncthreads();
+    if (sizeof(T) == 8 || (++chunk & 3) == 0) {
+#pragma unroll
+      for (int a = 0; a < BS; a++)
+#pragma unroll
+        for (int b = 0; b < BS; b++) {
+          acc[a][b] += (double)accs[a][b];
+          accs[a][b] = T(0);
+        }
+    }
+  }
+  if (!active) return;
+  double* out = partial + (size_t)blockIdx.z * h * h;
+#pragma unroll
+  for (int a = 0; a < BS; a++)
+#pragma unroll
+    for (int b = 0; b < BS; b++) {
+      const int i = BS * bi + a, j = BS * bj + b;
+      if (i < h && j <= i) out[(size_t)j * h + i] = acc[a][b] + (double)accs[a][b];
+    }
+}
+
+// G (h x h) from the lower-triangle partials, both triangles
+__global__ void gram_sym_reduce_kernel(const double* __restrict__ partial, int splits, int h,
+                                       double* __restrict__ G, int ldg)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= h * h) return;
+  int i = e % h, j = e / h;
+  const int src = i >= j ? e : j + i * h;
+  double s = 0.0;
+  for (int p = 0; p < splits; p++) s += partial[(size_t)p * h * h + src];
+  G[(size_t)j * ldg + i] = s;
+}
+
+// the row splits of gram_launch for a single (gx = gy = 1) output tile
+static long gram_splits(gpu_Context* ctx, long n, long* rows)
+{
+  long splits = 2 * ctx->num_sms;
+  long max_splits = (n + 255) / 256;
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  long r = (n + splits - 1) / splits;
+  r = (r + 31) / 32 * 32;
+  splits = (n + r - 1) / r;
+  if (splits < 1) splits = 1;
+  *rows = r;
+  return splits;
+}
+
+template <typename T, int BS>
+static int gram_sym_launch(gpu_Context* ctx, long n, const blk_cols* X, int h, double* G, int ldg)
+{
+  long rows;
+  const long splits = gram_splits(ctx, n, &rows);
+  double* partial = (double*)gb_workspace(ctx, sizeof(double) * (size_t)splits * h * h);
+  if (!partial) return -1;
+  const int nb = (h + BS - 1) / BS;
+  const int threads = (nb * (nb + 1) / 2 + 31) / 32 * 32;
+  dim3 grid(1, 1, (unsigned)splits);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, sizeof(T) == 8 ? GB_K_GRAM : GB_K_GRAM32);
+  gram_sym_partial_kernel<T, BS><<<grid, threads, 0, S(ctx)>>>(*X, h, n, rows, partial);
+  gram_sym_reduce_kernel<<<(h * h + 255) / 256, 256, 0, S(ctx)>>>(partial, (int)splits, h, G, ldg);
+  gb_prof_end(ctx, &pr, (double)sizeof(T) * n * h, (double)n * h * (h + 1));
+  gb_count_launch(2);
+  return CUDA_LAUNCH_CHECK(ctx, "gram_sym");
+}
+
 template <typename T, int TM, int TN>
 static int gram_launch(gpu_Context* ctx, long n, const blk_cols* X, int h, const blk_cols* Y,
                        int w, double* G, int ldg)
@@ -143,6 +272,14 @@ extern "C" int gb_gram(gpu_Context* ctx, int dtype, long n, const blk_cols* X, i
                        const blk_cols* Y, int w, double* G, int ldg)
 {
   if (h <= 0 || w <= 0) return 0;
+  // X'X with h <= 64 (one output tile): the lower triangle only
+  if (h == w && h <= 64 && memcmp(X->col, Y->col, sizeof(void*) * (size_t)h) == 0) {
+    if (dtype == GPU_MV_FLOAT64)
+      return h <= 32 ? gram_sym_launch<double, 1>(ctx, n, X, h, G, ldg)
+                     : gram_sym_launch<double, 2>(ctx, n, X, h, G, ldg);
+    return h <= 32 ? gram_sym_launch<float, 1>(ctx, n, X, h, G, ldg)
+                   : gram_sym_launch<float, 2>(ctx, n, X, h, G, ldg);
+  }
   if (dtype == GPU_MV_FLOAT64) {
     if (h <= 32 && w <= 32) return gram_launch<double, 2, 2>(ctx, n, X, h, Y, w, G, ldg);
     return gram_launch<double, 4, 4>(ctx, n, X, h, Y, w, G, ldg);
@@ -154,11 +291,15 @@ extern "C" int gb_gram(gpu_Context* ctx, int dtype, long n, const blk_cols* X, i
 // ------------------------------------------------------------------------
 // X*C update: Y(:, j0:j0+32) for 64 rows per CTA; thread t owns row t%64
 // and 8 columns (t/64)*8 ... ; K staged 32 at a time in shared memory.
+// tri: C is upper triangular with explicit zeros below the diagonal (a
+// Cholesky-QR factor); a warp stops at its last column's diagonal, skipping
+// only terms that add an exact zero, so Y is bit-identical to the full
+// product.
 // ------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) bymat_kernel(blk_cols X, int h, const double* __restrict__ C,
                                                     int ldc, blk_cols Y, int w, blk_cols Z,
-                                                    int has_z, long n)
+                                                    int has_z, long n, int tri)
 {
   constexpr int BM = 64, BN = 32, KC = 32;
   __shared__ T xs[KC][BM];
@@ -171,7 +312,8 @@ __global__ void __launch_bounds__(256) bymat_kernel(blk_cols X, int h, const dou
 #pragma unroll
   for (int b = 0; b < 8; b++) acc[b] = T(0);
 
-  for (int k0 = 0; k0 < h; k0 += KC) {
+  const int kmax = tri ? min(h, j0 + BN) : h;
+  for (int k0 = 0; k0 < kmax; k0 += KC) {
     for (int e = t; e < KC * BM; e += 256) {
       int rr = e % BM, kk = e / BM;
       long r = r0 + rr;
@@ -186,8 +328,9 @@ __global__ void __launch_bounds__(256) bymat_kernel(blk_cols X, int h, const dou
       cs[kk][jj] = v;
     }
     __syncthreads();
+    const int kk_end = tri ? max(0, min(KC, j0 + cg * 8 + 8 - k0)) : KC;
 #pragma unroll 8
-    for (int kk = 0; kk < KC; kk++) {
+    for (int kk = 0; kk < kk_end; kk++) {
       T xv = xs[kk][rl];
 #pragma unroll
       for (int b = 0; b < 8; b++) acc[b] = fma(xv, cs[kk][cg * 8 + b], acc[b]);
@@ -208,8 +351,9 @@ __global__ void __launch_bounds__(256) bymat_kernel(blk_cols X, int h, const dou
   }
 }
 
-extern "C" int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
-                        const double* C, int ldc, const blk_cols* Y, int w, const blk_cols* Z)
+static int bymat_launch(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
+                        const double* C, int ldc, const blk_cols* Y, int w, const blk_cols* Z,
+                        int tri)
 {
   if (w <= 0 || n <= 0) return 0;
   dim3 grid((unsigned)((n + 63) / 64), (w + 31) / 32);
@@ -219,12 +363,27 @@ extern "C" int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, 
   gb_prof_rec pr;
   gb_prof_begin(ctx, &pr, dtype == GPU_MV_FLOAT64 ? GB_K_XC : GB_K_XC32);
   if (dtype == GPU_MV_FLOAT64)
-    bymat_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n);
+    bymat_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n, tri);
   else
-    bymat_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n);
-  gb_prof_end(ctx, &pr, es * n * (h + w + (Z ? w : 0)), 2.0 * n * h * w);
+    bymat_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, h, C, ldc, *Y, w, *z, Z != NULL, n, tri);
+  // a triangular C: sum over j of min(j + 1, h) products per row
+  const double kw = tri ? (double)w * (w + 1) / 2 - (w > h ? (double)(w - h) * (w - h + 1) / 2 : 0.0)
+                        : (double)h * w;
+  gb_prof_end(ctx, &pr, es * n * (h + w + (Z ? w : 0)), 2.0 * n * kw);
   gb_count_launch(1);
   return CUDA_LAUNCH_CHECK(ctx, "bymat");
+}
+
+extern "C" int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
+                        const double* C, int ldc, const blk_cols* Y, int w, const blk_cols* Z)
+{
+  return bymat_launch(ctx, dtype, n, X, h, C, ldc, Y, w, Z, 0);
+}
+
+extern "C" int gb_bymat_tri(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h,
+                            const double* C, int ldc, const blk_cols* Y, int w)
+{
+  return bymat_launch(ctx, dtype, n, X, h, C, ldc, Y, w, NULL, 1);
 }
 
 // ------------------------------------------------------------------------

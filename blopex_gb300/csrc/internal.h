@@ -117,6 +117,9 @@ int gb_gram(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h, const
 /* Y(:,j) = sum_i X(:,i) C(i,j) [+ Z(:,j)], C FP64 device column-major (ldc) */
 int gb_bymat(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h, const double* C,
              int ldc, const blk_cols* Y, int w, const blk_cols* Z);
+/* the same with C upper triangular (explicit zeros below the diagonal) */
+int gb_bymat_tri(gpu_Context* ctx, int dtype, long n, const blk_cols* X, int h, const double* C,
+                 int ldc, const blk_cols* Y, int w);
 /* Y(:,j) = alpha * X(:,j) + beta * Y(:,j) for j < w */
 int gb_axpby(gpu_Context* ctx, int dtype, long n, double alpha, const blk_cols* X, double beta,
              const blk_cols* Y, int w);

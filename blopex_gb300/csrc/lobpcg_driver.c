@@ -125,6 +125,17 @@ static int d_bymat(solver_t* s, gpu_MultiVector* x, const double* C, int ldc, gp
   return gb_bymat(s->ctx, x->dtype, s->n, &a, x->num_active, C, ldc, &b, y->num_active, NULL);
 }
 
+/* the same with C upper triangular (a Cholesky-QR factor from gb_cholqr_factor,
+   zeros below the diagonal) */
+static int d_bymat_tri(solver_t* s, gpu_MultiVector* x, const double* C, int ldc,
+                       gpu_MultiVector* y)
+{
+  blk_cols a, b;
+  cols(x, &a);
+  cols(y, &b);
+  return gb_bymat_tri(s->ctx, x->dtype, s->n, &a, x->num_active, C, ldc, &b, y->num_active);
+}
+
 /* apply an operator callback to the active columns of x -> y */
 static int d_apply(solver_t* s, op_fn op, void* data, gpu_MultiVector* x, gpu_MultiVector* y)
 {
@@ -191,7 +202,7 @@ static int d_implicit_qr(solver_t* s, gpu_MultiVector* x, gpu_MultiVector* bx, d
   if (read_info(s, info)) return -1;
   if (*info) return 0;
   if (d_copy(s, x, z)) return -1;
-  return d_bymat(s, z, r, ld, x);
+  return d_bymat_tri(s, z, r, ld, x);
 }
 
 static int d_sygv(solver_t* s, int m, double* w, int* info)
@@ -431,7 +442,7 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
       if (s->verbosity) printf("DPOTRF INFO = %d\n", exitflag);
       break;
     }
-    if (!s->noB && (d_bymat(s, s->BR, upR, k3, s->W) || d_copy(s, s->W, s->BR))) return -2;
+    if (!s->noB && (d_bymat_tri(s, s->BR, upR, k3, s->W) || d_copy(s, s->W, s->BR))) return -2;
     if (d_apply(s, s->A, s->Adata, s->R, s->AR)) return -2;
 
     if (*it > ctl->it_base + 1) {
@@ -442,8 +453,8 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
       if (exitflag) {
         sizeP = 0; /* lobpcg.c:1056-1063 */
       } else {
-        if (!s->noB && (d_bymat(s, s->BP, upP, k3, s->W) || d_copy(s, s->W, s->BP))) return -2;
-        if (d_bymat(s, s->AP, upP, k3, s->W) || d_copy(s, s->W, s->AP)) return -2;
+        if (!s->noB && (d_bymat_tri(s, s->BP, upP, k3, s->W) || d_copy(s, s->W, s->BP))) return -2;
+        if (d_bymat_tri(s, s->AP, upP, k3, s->W) || d_copy(s, s->W, s->AP)) return -2;
       }
     } else {
       sizeP = 0;

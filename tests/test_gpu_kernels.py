@@ -47,6 +47,32 @@ def test_gram_matches_numpy(ctx, dtype, rtol, n, h, w):
     ctx.lib.mv_MultiVectorDestroy(yy)
 
 
+@pytest.mark.parametrize("dtype", [S.FLOAT64, S.FLOAT32])
+@pytest.mark.parametrize("n,h", [(1, 1), (300, 7), (4099, 32), (70001, 33), (20000, 64)])
+def test_symmetric_gram_bit_identical(ctx, dtype, n, h):
+    """X'X of one block takes the lower-triangle kernel; the same product of
+    two distinct copies takes the full kernel.  Same splits, same order of
+    multiply-adds: the results agree bit for bit, and X'X is symmetric."""
+    rng = np.random.default_rng(n * 7 + h)
+    x = rng.standard_normal((n, h))
+    X = S.MultiVector.from_host(ctx, x, dtype)
+    X2 = S.MultiVector.from_host(ctx, x, dtype)
+    interp = S._Interp(ctx.lib)
+    xx = ctx.lib.mv_MultiVectorWrap(interp.ptr, X.handle, 0)
+    x2 = ctx.lib.mv_MultiVectorWrap(interp.ptr, X2.handle, 0)
+    sym = np.zeros((h, h), order="F")
+    full = np.zeros((h, h), order="F")
+    ctx.lib.mv_MultiVectorByMultiVector(xx, xx, h, h, h, sym.ctypes.data)
+    ctx.lib.mv_MultiVectorByMultiVector(xx, x2, h, h, h, full.ctypes.data)
+    ctx.lib.mv_MultiVectorDestroy(xx)
+    ctx.lib.mv_MultiVectorDestroy(x2)
+    assert np.array_equal(sym, np.tril(full) + np.tril(full, -1).T)
+    assert np.array_equal(sym, full)
+    xr = x.astype(np.float32).astype(np.float64) if dtype == S.FLOAT32 else x
+    np.testing.assert_allclose(sym, xr.T @ xr, rtol=0,
+                               atol=(1e-13 if dtype == S.FLOAT64 else 2e-5) * n)
+
+
 @pytest.mark.parametrize("dtype,rtol", [(S.FLOAT64, 1e-13), (S.FLOAT32, 2e-5)])
 @pytest.mark.parametrize("n,h,w", [(5, 1, 1), (1000, 10, 10), (70001, 40, 33)])
 def test_bymatrix_matches_numpy(ctx, dtype, rtol, n, h, w):
