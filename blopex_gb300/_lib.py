@@ -30,7 +30,7 @@ class Options(ctypes.Structure):
                 ("sygv_fail_at", c_int), ("explicit_pivot_below", c_double),
                 ("fp32_accurate_op", c_int), ("recompute_ap", c_int), ("explicit_fp64", c_int),
                 ("accum64", c_int),
-                ("rr_method", c_int)]
+                ("rr_method", c_int), ("fp32_precond", c_int)]
 
 
 class Stats(ctypes.Structure):

@@ -60,6 +60,7 @@ static void default_options(lobpcg_gpu_options* o)
   o->accum64 = 1;
   o->fp32_accurate_op = 0;
   o->recompute_ap = 1;
+  o->fp32_precond = 0;
   o->explicit_pivot_below = 1e-6;
   o->fp32_stall = 20;
   o->tensor_cores = 1;

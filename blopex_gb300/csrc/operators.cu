@@ -43,6 +43,7 @@ struct gpu_Operator {
   gpu_Operator* prec;
   int iters;
   gpu_MultiVector* work[4];  // r, z, p, q
+  gpu_MultiVector* io32[2];  // FP32 copies of an FP64 input / output (mixed mode)
   double* coef;              // 4 x BLK_MAXCOLS device doubles
 };
 
@@ -451,6 +452,7 @@ extern "C" void gpu_OperatorDestroy(gpu_Operator* op)
   gb_device_free(op->d);
   gb_device_free(op->d32);
   for (int b = 0; b < 4; b++) gpu_MultiVectorDestroy(op->work[b]);
+  for (int b = 0; b < 2; b++) gpu_MultiVectorDestroy(op->io32[b]);
   gb_device_free(op->coef);
   free(op);
 }
@@ -1085,6 +1087,33 @@ static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
   if (X->size != op->n || Y->size != op->n || Y->num_active != w || X->dtype != Y->dtype)
     return gb_fail(ctx, "PCG preconditioner: block shapes");
   if (w == 0) return 0;
+  if (X->dtype == GPU_MV_FLOAT64 && ctx->opt.precision == LOBPCG_GPU_MIXED &&
+      ctx->opt.fp32_precond) {
+    // mixed mode, FP64 block: the inner iteration on FP32 copies.  The
+    // preconditioner only shapes the search direction T r (the solver's
+    // residuals and Ritz pairs stay FP64), and on this GPU an FP64 operator
+    // application is FP64-pipe bound where the FP32 one is HBM bound.
+    gpu_MultiVector** io = op->io32;
+    if (!io[0] || io[0]->num_vectors < w) {
+      for (int b = 0; b < 2; b++) {
+        gpu_MultiVectorDestroy(io[b]);
+        io[b] = gpu_MultiVectorCreate(ctx, op->n, w, GPU_MV_FLOAT32);
+        if (!io[b]) return -1;
+      }
+    }
+    int mask[BLK_MAXCOLS];
+    for (int c = 0; c < io[0]->num_vectors; c++) mask[c] = c < w;
+    gb_mv_set_mask_host(io[0], mask);
+    gb_mv_set_mask_host(io[1], mask);
+    blk_cols cx, cy, c0, c1;
+    gb_mv_fill_cols(X, &cx, 0);
+    gb_mv_fill_cols(Y, &cy, 0);
+    gb_mv_fill_cols(io[0], &c0, 0);
+    gb_mv_fill_cols(io[1], &c1, 0);
+    if (gb_convert(ctx, op->n, GPU_MV_FLOAT64, &cx, GPU_MV_FLOAT32, &c0, w)) return -1;
+    if (pcg_apply(op, io[0], io[1])) return -1;
+    return gb_convert(ctx, op->n, GPU_MV_FLOAT32, &c1, GPU_MV_FLOAT64, &cy, w);
+  }
   // work blocks of (at least) this width and dtype
   gpu_MultiVector** wk = op->work;
   if (!wk[0] || wk[0]->dtype != X->dtype || wk[0]->num_vectors < w) {

@@ -56,6 +56,9 @@ typedef struct {
                                bisection and inverse iteration (default); 1 = one-CTA FP64
                                Jacobi; 2 = FP32 Jacobi + FP64 refinement (order <= 192).
                                1 is also the fallback of 0 and 2. */
+  int fp32_precond;         /* mixed: the inner-CG preconditioner (gpu_PCGPreconditionerCreate)
+                               iterates on FP32 copies of FP64 blocks (the FP64 phase); the
+                               preconditioner only shapes the search directions (0) */
 } lobpcg_gpu_options;
 
 typedef struct {
