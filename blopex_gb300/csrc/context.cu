@@ -57,7 +57,7 @@ static void default_options(lobpcg_gpu_options* o)
   o->precision = LOBPCG_GPU_FP64;
   o->compensated_below = 1e-6;
   o->fp64_below = 0.0;
-  o->accum64 = 1;
+  o->accum64 = 0;
   o->fp32_accurate_op = 0;
   o->recompute_ap = 1;
   o->fp32_precond = 0;

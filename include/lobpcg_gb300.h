@@ -51,7 +51,8 @@ typedef struct {
   int explicit_fp64;        /* diagnostics: run the mixed mode's explicit-Gram phase on FP64
                                blocks (CUDA-core kernels), to separate algorithm from precision */
   int accum64;              /* mixed, tensor-core path: carry X and A X in FP64 through the FP32
-                               phase, adding FP32 corrections (1, default) */
+                               phase, adding FP32 corrections (0: measured no faster to 1e-8,
+                               and its FP64 streams cost ~40 % per FP32 iteration) */
   int rr_method;            /* Rayleigh-Ritz solver: 0 = FP64 Householder tridiagonalisation,
                                bisection and inverse iteration (default); 1 = one-CTA FP64
                                Jacobi; 2 = FP32 Jacobi + FP64 refinement (order <= 192).

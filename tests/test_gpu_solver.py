@@ -199,3 +199,48 @@ def test_rayleigh_ritz_paths_agree(ctx, name):
     if out[0].flag == 0:
         for r in out[1:]:
             np.testing.assert_allclose(out[0].lam, r.lam, rtol=max(1e-10, 3 * _spread(g)))
+
+
+@pytest.mark.parametrize("fp32_precond", [0, 1])
+def test_mixed_inner_cg_preconditioner(ctx, fp32_precond):
+    """Mixed mode with the inner-CG preconditioner (HYPRE -pcgitr semantics):
+    with the FP64 phase's preconditioner on FP32 copies or in FP64, the solve
+    meets the tolerance and its eigenvalues agree with the FP64 solve's."""
+    cx, cy, cz = P.stencil7_coefficients(16, 16, 16, seed=4)
+    A = S.Stencil7(ctx, cx, cy, cz)
+    T = S.PCGPreconditioner(ctx, A, S.Diagonal(ctx, 1.0 / A.diagonal()), 5)
+    x0 = P.drand48_block(16 ** 3, 6, 3)
+    res = {}
+    for prec in (S.FP64, S.MIXED):
+        ctx.set_options(precision=prec, fp32_precond=fp32_precond)
+        try:
+            X = S.MultiVector.from_host(ctx, x0)
+            res[prec] = S.lobpcg_solve_double(X, A, T=T, atol=1e-8, rtol=1e-50, maxit=300)
+        finally:
+            ctx.set_options(precision=S.FP64, fp32_precond=0)
+    for r in res.values():
+        assert r.flag == 0, ctx.last_error()
+        assert np.max(r.res) <= 1e-8
+    np.testing.assert_allclose(res[S.MIXED].lam, res[S.FP64].lam, rtol=1e-10)
+
+
+@pytest.mark.parametrize("opts", [dict(accum64=1), dict(recompute_ap=0), dict(explicit_fp64=1),
+                                  dict(fp32_accurate_op=1)])
+def test_mixed_phase_options(ctx, opts):
+    """The FP32 phase's alternative formulations (FP64 carry-through of X and
+    A X, A P by the block update, FP64 blocks, FP64 arithmetic for A R) all
+    reach the tolerance with the reference's eigenvalues."""
+    name = "st7vc_12_k6_jacobi"
+    g = load(name)
+    case = C.build(name)
+    case.maxit *= 3
+    ctx.set_options(precision=S.MIXED, **opts)
+    try:
+        r, _ = run_case(ctx, case)
+    finally:
+        ctx.set_options(precision=S.FP64, accum64=0, recompute_ap=1, explicit_fp64=0,
+                        fp32_accurate_op=0)
+    assert r.flag == 0, ctx.last_error()
+    tol = np.abs(r.lam) * case.rtol + case.atol + np.finfo(float).eps
+    assert np.all(r.res <= tol)
+    np.testing.assert_allclose(r.lam, g["lambda"], rtol=max(LAMBDA_RTOL, 3 * _spread(g)))
