@@ -64,15 +64,20 @@ struct rr_scratch {
 // so that the caller restarts without P); below RR_GRADED_BELOW, C is
 // graded beyond what the tridiagonal solver (absolute accuracy
 // eps |C|) resolves for the small eigenvalues, and the FP64 Jacobi solver
-// (relative accuracy on graded matrices) runs instead (status 7).
+// (relative accuracy on graded matrices) runs instead (status 7).  Up to
+// order RR_CHOL_SMEM_M the factorisation runs in shared memory, then L and
+// L' (row-major) are written out.
 #define RR_GRADED_BELOW 1e-10
+#define RR_CHOL_SMEM_M 160  // the factor in shared memory (m * m doubles) up to this order
+template <bool SMEM>
 __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __restrict__ B, int ld,
                                                                int m, rr_scratch s, int* info,
                                                                double report_below)
 {
+  extern __shared__ double Ls[];
   __shared__ int bad;
-  double* L = s.L64;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  double* L = SMEM ? Ls : s.L64;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   double qmin = HUGE_VAL;
   int jmin = 0;
   if (tid == 0) {
@@ -104,10 +109,10 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
     const double djj = L[j + (size_t)j * m];
     for (int i = j + 1 + tid; i < m; i += nt) L[i + (size_t)j * m] /= djj;
     __syncthreads();
-    const int r = m - j - 1;
-    for (int e = tid; e < r * r; e += nt) {
-      int i = j + 1 + e % r, l = j + 1 + e / r;
-      if (i >= l) L[i + (size_t)l * m] -= L[i + (size_t)j * m] * L[l + (size_t)j * m];
+    // trailing update, a warp per column: L(i, l) -= L(i, j) L(l, j), i >= l > j
+    for (int l = j + 1 + warp; l < m; l += nw) {
+      const double llj = L[l + (size_t)j * m];
+      for (int i = l + lane; i < m; i += 32) L[i + (size_t)l * m] -= L[i + (size_t)j * m] * llj;
     }
     __syncthreads();
   }
@@ -129,6 +134,7 @@ __global__ void __launch_bounds__(RR_THREADS) rr_chol64_kernel(const double* __r
   }
   for (int e = tid; e < m * m; e += nt) {
     int i = e % m, p = e / m;
+    if (SMEM) s.L64[e] = L[e];
     s.LT64[p + (size_t)i * m] = L[e];
   }
 }
@@ -1185,7 +1191,15 @@ static void rr_reduce(gpu_Context* ctx, double* A, double* B, int ld, int m, int
   gb_prof_rec ps;
   const double m3 = (double)m * m * m;
   const size_t mm = (size_t)m * m;
-  RR_STAGE(GB_K_RR_CHOL, m3 / 3, (rr_chol64_kernel<<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info, report_below)));
+  if (m <= RR_CHOL_SMEM_M) {
+    const int sm = (int)(sizeof(double) * (size_t)m * m);
+    cudaFuncSetAttribute(rr_chol64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    RR_STAGE(GB_K_RR_CHOL, m3 / 3,
+             (rr_chol64_kernel<true><<<1, RR_THREADS, sm, st>>>(B, ld, m, s, info, report_below)));
+  } else {
+    RR_STAGE(GB_K_RR_CHOL, m3 / 3,
+             (rr_chol64_kernel<false><<<1, RR_THREADS, 0, st>>>(B, ld, m, s, info, report_below)));
+  }
   RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm(st, 0, A, ld, s.W64, m, m, m, s)));
   RR_STAGE(GB_K_RR_TRSM, m3, (rr_trsm(st, 1, s.W64, m, s.C64, m, m, m, s)));
   if (jacobi32) rr_sym_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(m, s);
