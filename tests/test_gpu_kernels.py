@@ -100,6 +100,19 @@ def _ops(ctx):
     out = []
     rp, ci, va = P.laplacian3d_csr(9, 7, 5)
     out.append((S.CSRMatrix(ctx, rp, ci, va), O.csr(rp, ci, va), 315))
+    # rows of 1 to ~40 entries: the FP32 kernel's register path and its long-row loop
+    m = 300
+    dense = np.zeros((m, m))
+    for i in range(m):
+        cols = rng.choice(m, size=int(rng.integers(0, 20)), replace=False)
+        dense[i, cols] = rng.standard_normal(cols.size)
+    dense = dense + dense.T + np.diag(rng.uniform(1.0, 2.0, m))
+    rows, cols = np.nonzero(dense)
+    rp = np.searchsorted(rows, np.arange(m + 1)).astype(np.int32)
+    ci = cols.astype(np.int32)
+    va = dense[rows, cols]
+    assert np.diff(rp).max() > 8 and np.diff(rp).min() <= 8
+    out.append((S.CSRMatrix(ctx, rp, ci, va), O.csr(rp, ci, va), m))
     cx, cy, cz = P.stencil7_coefficients(11, 6, 5, seed=2)
     out.append((S.Stencil7(ctx, cx, cy, cz, 0.3), O.stencil7(11, 6, 5, cx, cy, cz, 0.3), 330))
     # several (x, y) tiles and z chunks of the blocked kernel, ragged edges
