@@ -247,14 +247,16 @@ def run_adjoint(args, cfg):
     from blopex_gb300 import adjoint as AD
     from blopex_gb300 import problems as P
     from blopex_gb300 import solver as S
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
     nx, ny = cfg["grid"]
     n, k = nx * ny, cfg["k"]
     theta = 0.5 * P.gaussian_random_field(nx, ny, 0.1, cfg["seed"])
     cx, cy = P.stencil5_from_cells(np.exp(theta))
     v = np.random.default_rng(cfg["seed"]).standard_normal(n)
     v /= np.linalg.norm(v)
-    ctx = S.Context(0)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    ctx = S.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     A = S.Stencil5(ctx, cx, cy)
     J = S.Diagonal(ctx, 1.0 / A.diagonal())
     T = S.PCGPreconditioner(ctx, A, J, cfg["inner_cg"])
@@ -289,7 +291,9 @@ def run_adjoint(args, cfg):
         backward(forward())
     ctx.profiling(True)
     ctx.reset_kernel_times()
-    sampler = ClockSampler(0)
+    sampler = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
     sampler.start()
     launches0 = ctx.lib.gpu_KernelLaunchCount()
     fwd, bwd, its, aits, res = [], [], 0, 0, 0.0
@@ -303,7 +307,8 @@ def run_adjoint(args, cfg):
     clocks = sampler.stop()
     kt = ctx.kernel_times()
     ctx.profiling(False)
-    tf, tb = statistics.median(fwd), statistics.median(bwd)
+    tf = max_over_ranks(statistics.median(fwd), dist, "cuda")
+    tb = max_over_ranks(statistics.median(bwd), dist, "cuda")
 
     # e2e: host theta -> torch autograd -> host gradient, every step
     opts = AD.SolveOptions(k=k, atol=cfg["tol"], maxit=cfg["maxit"], adjoint_tol=cfg["adjoint_tol"],
@@ -322,8 +327,9 @@ def run_adjoint(args, cfg):
         e2e.append((time.perf_counter() - t0) * 1e3)
     pk, _ = peaks()
     total = sum(v_["ms"] for v_ in kt.values()) or 1.0
+    e2e_ms = max_over_ranks(statistics.median(e2e), dist, "cuda")
     line = {"metric": "fwd+bwd ms (forward solve + reverse-mode gradient)", "value": tf + tb,
-            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": tf + tb, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["label"], "n": n, "k": k, "tol": cfg["tol"],
@@ -335,12 +341,15 @@ def run_adjoint(args, cfg):
             "kernels": {nm: {"share": x["ms"] / total, "launches": x["launches"],
                              "avg_ms": x["ms"] / x["launches"]}
                         for nm, x in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])[:8]},
-            "e2e": {"value": statistics.median(e2e), "unit": "ms",
+            "e2e": {"value": e2e_ms, "unit": "ms",
                     "h2d_bytes_per_step": 8 * (cx.size + cy.size),
                     "d2h_bytes_per_step": 8 * (n * k + k + cx.size + cy.size)},
             "gpu_launches": int(launches), "clocks": clocks,
             "roofline": None}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def run_reference(args, cfg):
@@ -361,6 +370,30 @@ def run_reference(args, cfg):
             "config": config_block(cfg, args), "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def dist_setup(backend: str = "nccl"):
+    """(world, rank, local rank, torch.distributed or None) from the torchrun
+    environment; a process group only when there is more than one rank."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def max_over_ranks(value: float, dist, device) -> float:
+    """The largest of the ranks' values, on every rank (the job's time with one
+    replica per rank); the value itself without a process group."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def metric_name(cfg):
@@ -415,13 +448,7 @@ def main():
         return
 
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
 
     from blopex_gb300 import solver as S
@@ -472,11 +499,7 @@ def main():
     barrier()
     ktimes = ctx.kernel_times()
     ctx.profiling(False)
-    secs = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    if dist is not None:
-        t = torch.tensor([secs], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
+    secs = max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps, dist, "cuda")
     res = results[-1]
 
     # e2e: X0 from pinned host memory, Ritz vectors back, every step
@@ -498,10 +521,8 @@ def main():
         X.download_ptr(pinned_out.data_ptr(), n)
         e2e_times.append(time.perf_counter() - t0)
     e2e = statistics.median(e2e_times) if e2e_times else None
-    if dist is not None and e2e is not None:
-        t = torch.tensor([e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = float(t.item())
+    if e2e is not None:
+        e2e = max_over_ranks(e2e, dist, "cuda")
 
     pk, pk_kind = peaks()
     fp64_peak = fp64_peak_tflops(torch)
