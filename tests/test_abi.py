@@ -57,3 +57,35 @@ def test_fortran_matrix_host_routines():
     assert lib.utilities_FortranMatrixHeight(blk) == 2 and lib.utilities_FortranMatrixWidth(blk) == 3
     lib.utilities_FortranMatrixDestroy(blk)
     lib.utilities_FortranMatrixDestroy(m)
+
+
+def _header_struct(name):
+    """[(field, C type)] of `typedef struct { ... } name;` in lobpcg_gb300.h."""
+    src = open(os.path.join(ROOT, "include", "lobpcg_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef\s+struct\s*\{((?:(?!typedef).)*?)\}\s*" + name + r"\s*;", src,
+                     re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        m = re.match(r"(.*?)\s*\b(\w+)\s*(\[\s*\d+\s*\])?$", decl)
+        out.append((m.group(2), m.group(1) + (m.group(3) or "")))
+    return out
+
+
+_CTYPES = {"int": ctypes.c_int, "double": ctypes.c_double, "long long": ctypes.c_longlong}
+
+
+def test_python_structs_mirror_the_header():
+    """The ctypes mirrors of the options and statistics structs have the
+    header's fields, in order and with the same types (a mismatch would
+    silently shift every later field)."""
+    for cname, py in (("lobpcg_gpu_options", _lib.Options), ("lobpcg_gpu_stats", _lib.Stats)):
+        fields = _header_struct(cname)
+        assert [f for f, _ in fields] == [f for f, _ in py._fields_], cname
+        for (f, ctype), (_, pytype) in zip(fields, py._fields_):
+            assert _CTYPES[ctype] is pytype, (cname, f, ctype, pytype)
+    kt = _header_struct("lobpcg_gpu_kernel_time")
+    assert [f for f, _ in kt] == [f for f, _ in _lib.KernelTime._fields_]
