@@ -10,12 +10,15 @@
 // coefficients are made on first use.  One thread per row/cell applies the
 // operator to up to 16 columns at once so the coefficients are read once per
 // 16 columns; the x gathers of a warp are coalesced along the row index.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "internal.h"
+#include "tc_common.cuh"
 
 enum { OPK_CSR = 1, OPK_ST7 = 2, OPK_ST5 = 3, OPK_ST27 = 4, OPK_DIAG = 5, OPK_PCG = 6 };
 
@@ -361,6 +364,159 @@ __global__ void __launch_bounds__(256) st7_ring_kernel(int nx, int ny, int nz,
   }
 }
 
+// ------------------------------------------- 7-point, FP32, TMA column ring
+// The column ring of st7_ring_kernel with the copies done by the tensor
+// memory accelerator: per column one thread issues three 4D tensor loads
+// (x, y, z, block column) on one mbarrier -- the 40 x 34 centre box from
+// (i0 - 4, j0 - 1, k) and the 32 x 32 boxes of planes k - 1 and k + 1 --
+// and TMA writes the same shared-memory layout the cp.async plan builds
+// (centre rows of 40 floats, cells at offsets 4-35), filling everything off
+// the grid with zeros.  x coordinates are multiples of 4 floats (16 bytes);
+// every box starts on a 128-byte boundary of its slot.  Waits are bounded: a
+// timeout stops the issue of further copies, poisons the CTA's outputs with
+// NaN, sets the context's device error word and, before the CTA exits,
+// waits (bounded again) for the copies still in flight.
+#define ST7T_DEPTH 3
+#define ST7T_BELOW 1376  // floats: the 34 x 40 centre box, padded to 128 bytes
+#define ST7T_ABOVE (ST7T_BELOW + 1024)
+#define ST7T_SLOT (ST7T_ABOVE + 1024)            // 13696 bytes, a multiple of 128
+#define ST7T_BYTES ((34 * 40 + 2 * 32 * 32) * 4)  // bytes per column (13632)
+
+struct st7t_cols {
+  int c[BLK_MAXCOLS];  // physical column of each active column
+};
+
+static __device__ __forceinline__ void st7t_load(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                                 int z, int c, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3, %4, %5}], [%6];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(c), "r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(256) st7_tma_kernel(
+    int nx, int ny, int nz, const float* __restrict__ cx, const float* __restrict__ cy,
+    const float* __restrict__ cz, float shift, const __grid_constant__ CUtensorMap tm_c,
+    const __grid_constant__ CUtensorMap tm_z, const __grid_constant__ st7t_cols XC,
+    const __grid_constant__ blk_cols Y, int w, int* err)
+{
+  __shared__ __align__(128) float ring[ST7T_DEPTH * ST7T_SLOT];
+  __shared__ __align__(8) uint64_t bar[ST7T_DEPTH];
+  __shared__ int abort_flag;
+  __shared__ int never_flag;
+  const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
+  const int tiles_x = (nx + 31) / 32, tiles_y = (ny + 31) / 32;
+  const long b = blockIdx.x;
+  const int tile = (int)(b % ((long)tiles_x * tiles_y));
+  const int k = (int)(b / ((long)tiles_x * tiles_y));
+  const int i0 = (tile % tiles_x) * 32, j0 = (tile / tiles_x) * 32;
+  const long plane = (long)nx * ny;
+  if (t == 0) {
+    abort_flag = 0;
+    never_flag = 0;
+    for (int q = 0; q < ST7T_DEPTH; q++) mbar_init(&bar[q], 1);
+  }
+  fence_proxy_async();
+  __syncthreads();
+  const uint32_t ring_s = smem_u32(ring);
+  int issued = 0, waited = 0;  // thread 0: columns issued / columns whose copies it saw land
+  if (t == 0) {
+    for (int c = 0; c < ST7T_DEPTH - 1 && c < w; c++) {
+      const uint32_t bq = smem_u32(&bar[c]), d = ring_s + 4u * ST7T_SLOT * c;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bq),
+                   "r"((uint32_t)ST7T_BYTES)
+                   : "memory");
+      st7t_load(d, &tm_c, i0 - 4, j0 - 1, k, XC.c[c], bq);
+      st7t_load(d + 4u * ST7T_BELOW, &tm_z, i0, j0, k - 1, XC.c[c], bq);
+      st7t_load(d + 4u * ST7T_ABOVE, &tm_z, i0, j0, k + 1, XC.c[c], bq);
+      issued++;
+    }
+  }
+
+  // coefficients of the thread's four cells (rows j0 + 4 ty .. + 3)
+  const int i = i0 + tx, jb = j0 + 4 * ty;
+  float dg[4], ww[4], we[4], ws[4], wn[4], wb[4], wt[4];
+  bool valid[4];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const int j = jb + s;
+    valid[s] = i < nx && j < ny;
+    dg[s] = ww[s] = we[s] = ws[s] = wn[s] = wb[s] = wt[s] = 0.f;
+    if (valid[s]) {
+      const long cell = (long)i + (long)nx * j + plane * k;
+      const long jk = (long)j + (long)ny * k;
+      const float cw = cx[i + (long)(nx + 1) * jk];
+      const float ce = cx[i + 1 + (long)(nx + 1) * jk];
+      const float cs = cy[i + (long)nx * (j + (long)(ny + 1) * k)];
+      const float cn = cy[i + (long)nx * (j + 1 + (long)(ny + 1) * k)];
+      const float cb = cz[cell];
+      const float ct = cz[cell + plane];
+      dg[s] = cw + ce + cs + cn + cb + ct + shift;
+      ww[s] = i > 0 ? cw : 0.f;
+      we[s] = i < nx - 1 ? ce : 0.f;
+      ws[s] = j > 0 ? cs : 0.f;
+      wn[s] = j < ny - 1 ? cn : 0.f;
+      wb[s] = k > 0 ? cb : 0.f;
+      wt[s] = k < nz - 1 ? ct : 0.f;
+    }
+  }
+  const long cell0 = (long)i + (long)nx * jb + plane * k;
+
+  int slot = 0, ahead_slot = ST7T_DEPTH - 1;
+#pragma unroll 1
+  for (int col = 0; col < w; col++) {
+    const uint32_t parity = (uint32_t)((col / ST7T_DEPTH) & 1);
+    const bool ok = !abort_flag && mbar_wait(&bar[slot], parity, &abort_flag);
+    if (!ok) abort_flag = 1;
+    else if (t == 0) waited = col + 1;
+    __syncthreads();  // column col landed; every thread is done with the slot of col - 1
+    const bool go = !abort_flag;
+    const int ahead = col + ST7T_DEPTH - 1;
+    if (go && t == 0 && ahead < w) {
+      const uint32_t bq = smem_u32(&bar[ahead_slot]), d = ring_s + 4u * ST7T_SLOT * ahead_slot;
+      fence_proxy_async();
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bq),
+                   "r"((uint32_t)ST7T_BYTES)
+                   : "memory");
+      st7t_load(d, &tm_c, i0 - 4, j0 - 1, k, XC.c[ahead], bq);
+      st7t_load(d + 4u * ST7T_BELOW, &tm_z, i0, j0, k - 1, XC.c[ahead], bq);
+      st7t_load(d + 4u * ST7T_ABOVE, &tm_z, i0, j0, k + 1, XC.c[ahead], bq);
+      issued++;
+    }
+    float* y = (float*)Y.col[col] + cell0;
+    if (go) {
+      const float* sl = ring + ST7T_SLOT * slot;
+      float cv[6];
+#pragma unroll
+      for (int r = 0; r < 6; r++) cv[r] = sl[(4 * ty + r) * 40 + 4 + tx];
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        const int m = (4 * ty + 1 + s) * 40 + 4 + tx;
+        const float v1 = sl[m - 1], v2 = sl[m + 1];
+        const float v5 = sl[ST7T_BELOW + (4 * ty + s) * 32 + tx];
+        const float v6 = sl[ST7T_ABOVE + (4 * ty + s) * 32 + tx];
+        if (valid[s])
+          __stcs(y + (long)nx * s, dg[s] * cv[s + 1] - ww[s] * v1 - we[s] * v2 - ws[s] * cv[s] -
+                                       wn[s] * cv[s + 2] - wb[s] * v5 - wt[s] * v6);
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < 4; s++)
+        if (valid[s]) y[(long)nx * s] = __int_as_float(0x7fc00000);  // NaN: output incomplete
+    }
+    slot = slot == ST7T_DEPTH - 1 ? 0 : slot + 1;
+    ahead_slot = ahead_slot == ST7T_DEPTH - 1 ? 0 : ahead_slot + 1;
+  }
+  if (t == 0 && abort_flag) {
+    atomicExch(err, 1);
+    // copies issued but not seen landing: wait for them before the CTA exits
+    for (int c = waited; c < issued; c++)
+      mbar_wait(&bar[c % ST7T_DEPTH], (uint32_t)((c / ST7T_DEPTH) & 1), &never_flag);
+  }
+}
+
 // ------------------------------------------------------------ 5-point
 template <typename T>
 __global__ void __launch_bounds__(256) st5_kernel(int nx, int ny, const T* __restrict__ cx,
@@ -660,6 +816,48 @@ static int st7_ring_ok(const gpu_Operator* op, const blk_cols* xc, int w)
   return 1;
 }
 
+// the tensor-map encoder of the driver, found once through the runtime
+static PFN_cuTensorMapEncodeTiled_v12000 st7t_encoder(void)
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = NULL;
+  static int tried = 0;
+  if (!tried) {
+    tried = 1;
+    void* p = NULL;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// tensor maps of the FP32 block X as (x, y, z, column) for st7_tma_kernel:
+// boxes 40 x 34 (centre plane with halo) and 32 x 32 (planes above and
+// below).  TMA needs 16-byte-aligned bases and strides: nx a multiple of 4
+// and ld * 4 a multiple of 16.  Returns 0 when both maps were encoded.
+static int st7t_maps(const gpu_Operator* op, const gpu_MultiVector* X, CUtensorMap* mc,
+                     CUtensorMap* mz)
+{
+  PFN_cuTensorMapEncodeTiled_v12000 enc = st7t_encoder();
+  if (!enc || op->nx % 4 || ((uintptr_t)X->data & 15) || (X->ld * 4) % 16) return -1;
+  const cuuint64_t dims[4] = {(cuuint64_t)op->nx, (cuuint64_t)op->ny, (cuuint64_t)op->nz,
+                              (cuuint64_t)X->num_vectors};
+  const cuuint64_t strides[3] = {(cuuint64_t)op->nx * 4, (cuuint64_t)op->nx * op->ny * 4,
+                                 (cuuint64_t)X->ld * 4};
+  const cuuint32_t boxc[4] = {40, 34, 1, 1}, boxz[4] = {32, 32, 1, 1}, es[4] = {1, 1, 1, 1};
+  if (enc(mc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, X->data, dims, strides, boxc, es,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return -1;
+  if (enc(mz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, X->data, dims, strides, boxz, es,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return -1;
+  return 0;
+}
+
 static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
 
 extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
@@ -739,13 +937,20 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
                                                                op->vals, xc, yc, w);
       break;
     case OPK_ST7: {
+      CUtensorMap tmc, tmz;
       const unsigned tb = (unsigned)(((op->nx + ST_TX - 1) / ST_TX) * ((op->ny + ST_TY - 1) / ST_TY) *
                                      (long)op->nz);
       if (acc64)
         st7_kernel<float, double><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0],
                                                                     op->c[1], op->c[2], op->shift,
                                                                     xc, yc, w);
-      else if (f32 && st7_ring_ok(op, &xc, w))
+      else if (f32 && st7t_maps(op, X, &tmc, &tmz) == 0) {
+        st7t_cols pc;
+        for (int c = 0; c < w; c++) pc.c[c] = X->active[c];
+        st7_tma_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
+                         0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1], op->c32[2],
+                                      (float)op->shift, tmc, tmz, pc, yc, w, ctx->dcount + 5);
+      } else if (f32 && st7_ring_ok(op, &xc, w))
         st7_ring_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
                           0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
                                                 op->c32[2], (float)op->shift, xc, yc, w);
