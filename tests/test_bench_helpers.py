@@ -1,0 +1,51 @@
+"""CPU checks of the bench's roofline arithmetic: which roof bounds a kernel
+class, what `achieved` and `frac` are, and which traffic entries apply."""
+import json
+
+import bench
+
+
+def _v(ms, bytes_, flops, launches=10):
+    return {"ms": ms, "bytes": bytes_, "flops": flops, "launches": launches}
+
+
+def test_fp64_class_is_bound_by_the_fp64_pipe():
+    # 1 TFLOP in 1 s on a 1.1 TF/s FP64 pipe; its bytes would take far less at 6.8 TB/s
+    e = bench.roofline_entry("gram", _v(1000.0, 1e11, 1e12), 6800.0, 1.1, {})
+    assert e["bound"] == "fp64" and e["unit"] == "TFLOP/s"
+    assert abs(e["achieved"] - 1.0) < 1e-12 and abs(e["frac"] - 1.0 / 1.1) < 1e-12
+    assert e["avg_launch_ms"] == 100.0 and e["algorithmic_flops_per_launch"] == 1e11
+
+
+def test_fp32_class_is_never_taken_for_an_fp64_one():
+    # the same numbers under the FP32 class name: HBM-bound, achieved in GB/s
+    e = bench.roofline_entry("gram_fp32", _v(1000.0, 1e11, 1e12), 6800.0, 1.1, {})
+    assert e["bound"] == "hbm" and e["unit"] == "GB/s"
+    assert abs(e["achieved"] - 100.0) < 1e-9 and abs(e["frac"] - 100.0 / 6800.0) < 1e-12
+
+
+def test_tensor_class_bound_by_the_tensor_rate_only_when_slower_than_hbm():
+    hbm = bench.roofline_entry("tc_gram", _v(1.0, 6.8e9, 1e9), 6800.0, 1.1, {},
+                               fp64_arith=False, tf32_peak=960.0)
+    assert hbm["bound"] == "hbm" and abs(hbm["frac"] - 1.0) < 1e-9
+    ten = bench.roofline_entry("tc_gram", _v(1.0, 1e6, 9.6e11), 6800.0, 1.1, {},
+                               fp64_arith=False, tf32_peak=960.0)
+    assert ten["bound"] == "tensor" and abs(ten["frac"] - 1.0) < 1e-9
+
+
+def test_traffic_entries_are_filtered_by_workload(tmp_path, monkeypatch):
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    (prof / "traffic.json").write_text(json.dumps({
+        "gram": {"bytes_per_launch": 123, "config": "c2"},
+        "stencil7_fp32": {"bytes_per_launch": 456, "config": "c3"}}))
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert set(bench.load_traffic("c2")) == {"gram"}
+    assert set(bench.load_traffic("c3")) == {"stencil7_fp32"}
+    e = bench.roofline_entry("gram", _v(1000.0, 1e11, 1e12), 6800.0, 1.1, bench.load_traffic("c2"))
+    assert e["traffic"] == 123
+
+
+def test_committed_traffic_file_names_its_workloads():
+    traffic = bench.load_traffic("c2")
+    assert "gram" in traffic and traffic["gram"]["bytes_per_launch"] > 0
