@@ -89,3 +89,23 @@ def test_python_structs_mirror_the_header():
             assert _CTYPES[ctype] is pytype, (cname, f, ctype, pytype)
     kt = _header_struct("lobpcg_gpu_kernel_time")
     assert [f for f, _ in kt] == [f for f, _ in _lib.KernelTime._fields_]
+
+
+def test_c_caller_compiles_and_links(tmp_path):
+    """A C99 program calling lobpcg_solve_double the reference driver's way
+    (tests/c/serial_driver_gb300.c) compiles warning-free against include/
+    and links against the library: the headers are plain C and every symbol
+    a C caller uses resolves.  (Running it needs the GPU.)"""
+    import shutil
+    import subprocess
+    import pytest
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    libdir = os.path.dirname(_lib.LIBPATH)
+    exe = tmp_path / "serial_driver_gb300"
+    cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "c", "serial_driver_gb300.c"), "-L", libdir,
+           "-llobpcg_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert exe.exists()
