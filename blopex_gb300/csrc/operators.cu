@@ -7,9 +7,19 @@
 // (blopex_serial_double/pcg_multi/pcg_multi.c:167-193 MatMultiVec and
 // blopex_serial_double/matmultivec/matmultivec.c:11-48).
 // FP64 and FP32 multivectors are both accepted; FP32 copies of the
-// coefficients are made on first use.  One thread per row/cell applies the
-// operator to up to 16 columns at once so the coefficients are read once per
-// 16 columns; the x gathers of a warp are coalesced along the row index.
+// coefficients are made on first use.  Kernels, one thread per row or cell
+// with the x gathers of a warp coalesced along the row index:
+//   csr_kernel      CSR, 16 columns per pass over the row (FP64, and FP32
+//                   blocks with FP64 arithmetic);
+//   csr32_kernel    FP32 CSR: the row's entries in registers, the gathers of
+//                   four columns issued ahead of their products;
+//   st7_tma_kernel  FP32 7-point: plane tiles staged by TMA into a
+//                   shared-memory column ring (st7_ring_kernel: the same
+//                   with cp.async copies; st7_kernel: scalar, FP64 and the
+//                   unaligned cases);
+//   st5_kernel, st27_kernel, diag_kernel;
+// plus the inner-CG preconditioner (pcg_apply) and the parameter gradients
+// of the adjoint module (grad_*_kernel).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
