@@ -1,7 +1,9 @@
 // blockops.cu -- tall-skinny block kernels on column-major multivectors
 // (CUDA-core versions, FP64 and FP32 storage):
-//   Gram        G = X' Y          (serial_Multi_VectorInnerProd, multi_vector.c:354-406)
-//   X*C update  Y = X C [+ Z]     (serial_Multi_VectorByMatrix, multi_vector.c:474-524)
+//   Gram        G = X' Y          (serial_Multi_VectorInnerProd, multi_vector.c:354-406);
+//               X' X of one block on the lower triangle only, bit-identical
+//   X*C update  Y = X C [+ Z]     (serial_Multi_VectorByMatrix, multi_vector.c:474-524);
+//               C upper triangular: the zero triangle skipped, bit-identical
 //   axpby, column scaling, column dots, residual, precision conversion,
 //   drand48 fill (multi_vector.c:165-184).
 // Columns are addressed through blk_cols pointer tables, so masked
