@@ -153,6 +153,7 @@ SIGNATURES = {
     "gpu_ExplicitGram": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_int, c_void_p, c_void_p, c_int]),
     "gpu_BlockUpdate": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int]),
+    "gpu_SplitGram": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int]),
     "gpu_EigenvectorAdjoint": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_double, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),

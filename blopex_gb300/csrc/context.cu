@@ -17,7 +17,8 @@ static const char* k_names[GB_K_COUNT] = {"gram", "xc_update", "spmm_csr", "sten
                                           "rr_trsm64", "rr_jacobi32", "rr_gemm64", "rr_refine",
                                           "rr_tridiag", "rr_tridiag_eig", "gram_fp32",
                                           "xc_update_fp32", "spmm_csr_fp32", "stencil7_fp32",
-                                          "stencil5_fp32", "stencil27_fp32", "diag_scale_fp32"};
+                                          "stencil5_fp32", "stencil27_fp32", "diag_scale_fp32",
+                                          "oz_xc_update", "oz_gram"};
 
 
 extern "C" void gb_count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }

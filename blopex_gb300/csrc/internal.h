@@ -30,6 +30,8 @@ enum {
   GB_K_RR_EIG,
   /* the same operations with FP32 arithmetic (the mixed mode's FP32 phase) */
   GB_K_GRAM32, GB_K_XC32, GB_K_CSR32, GB_K_ST7_32, GB_K_ST5_32, GB_K_ST27_32, GB_K_DIAG32,
+  /* FP64-accurate split-operand products on the tensor cores */
+  GB_K_OZ_XC, GB_K_OZ_GRAM,
   GB_K_COUNT
 };
 
@@ -169,6 +171,19 @@ int gb_tc_gram(gpu_Context* ctx, long n, const blk_cols* X, int k, const blk_col
    columns, h <= 128, w <= 64, C FP64 on the device (leading dimension ldc) */
 int gb_tc_xc(gpu_Context* ctx, long n, const blk_cols* X, int h, const double* C, int ldc,
              const blk_cols* Y, int w, const blk_cols* Z);
+/* FP64-accurate Y = X C (+ Z) on the tensor cores by error-free splitting
+   (oz_xc.cu): X FP64 (h <= 64 columns, 16-byte aligned, readable up to an
+   even row count), C FP64 device (ldc), Y FP64 (w <= 64); Z optional, FP32
+   or FP64 (z_dtype); Y32 optional FP32 copy of Y */
+int gb_oz_xc(gpu_Context* ctx, long n, const blk_cols* X, int h, const double* C, int ldc,
+             const blk_cols* Y, int w, const blk_cols* Z, int z_dtype, const blk_cols* Y32);
+/* FP64-accurate Gram G = L' [L Q_0 Q_1 ...] on the tensor cores (oz_gram.cu):
+   L an FP64 block of h <= 64 columns; nq blocks Q_b of up to 64 columns each,
+   FP32 or FP64 (qdt[b]); every column 16-byte aligned and readable up to a
+   row count rounded to 4.  G (FP64 device, ldg) receives L'L in columns 0..h
+   and L'Q_b in the following columns, in order. */
+int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int nq, const blk_cols* Q,
+               const int* qw, const int* qdt, double* G, int ldg);
 /* device error word of the tensor-core kernels (0 = none); clears it */
 int gb_device_error(gpu_Context* ctx, int* err);
 

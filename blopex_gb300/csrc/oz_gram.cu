@@ -1,0 +1,470 @@
+// oz_gram.cu -- FP64-accurate Gram products G = L' [L Q_0 Q_1 ...] on the
+// tensor cores by error-free splitting (oz_common.cuh): L an FP64 block of
+// h <= 64 columns (the Ritz block X of the mixed mode), Q_b blocks of up to 64
+// FP32 or FP64 columns (R, P).  It is serial_Multi_VectorInnerProd
+// (blopex_serial_double/multivector/multi_vector.c:354-406; the X rows of
+// gramB, lobpcg.c:1105-1160) with exact accumulation: the FP32 tensor-core
+// accumulators round toward zero, and summed over millions of rows that
+// bias is ~1e-5 relative, while these rows of the Gram matrix must be right
+// to ~1e-9 for the mixed mode to reach residuals of 1e-8.
+//
+// The contraction runs over n rows in chunks of 64.  Within a chunk every
+// column has its own power-of-two scale and is cut into S = 4 balanced
+// 7-bit digits (28 fraction bits); level L = t + u of the digit products is
+// summed exactly in FP32 in TMEM (|sum| < 2^21).  After each chunk the four
+// levels are combined (FP32, round to nearest), scaled, and added into
+// double-float (hi + lo FP32) accumulators, so the chunk sums add without
+// bias; each CTA writes its sums in FP64 and a second kernel adds the CTAs
+// in a fixed order.
+//
+// Tile b of the grid pairs L with Q_b: the A operand has 128 rows, L's
+// columns in rows 0-63 and Q_b's in rows 64-127; the B operand is rows 0-63
+// of the same slices (L).  Per CTA (one per SM):
+//   warp 1          bulk-copies a chunk's columns (cp.async.bulk, 64 rows
+//                   each) into one of two raw buffers;
+//   warps 2-3, 12-15 find each column's chunk scale and write the digit
+//                   slices (128-byte-swizzled K-major, K = the chunk's rows);
+//   warp 0          allocates TMEM; one thread issues tcgen05.mma.kind::f16
+//                   (M = 128, N = 64, K = 16) for the pairs t + u < S into one
+//                   of two accumulator sets;
+//   warps 4-11      fold a finished chunk into the double-float sums (lane =
+//                   column of [L Q_b]; warps w and w + 4 share TMEM lanes and
+//                   take 32 of the 64 L columns each).
+// Every wait is bounded; a timeout sets an error word, the outputs become NaN.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "internal.h"
+#include "oz_common.cuh"
+
+#define OZG_S 4
+#define OZG_F (7 * OZG_S)
+#define OZG_THREADS 512
+#define OZG_NPROD 192
+#define OZG_ROWS 64                      // rows per chunk
+#define OZG_COLSTRIDE 528                // raw bytes per column (64 FP64 + 16 padding)
+#define OZG_RAW (128 * OZG_COLSTRIDE)    // one raw buffer
+#define OZG_SLICE 16384                  // 128 operand rows x 128 bytes
+#define OZG_SMEM (2 * OZG_RAW + OZG_S * OZG_SLICE + 1024)
+#define OZG_MAXQ 4  // 64 + 64 * OZG_MAXQ column slots fit blk_cols
+
+struct ozg_params {
+  blk_cols cols;       // tile b: L column c at cols.col[c]; Q_b column j at cols.col[64 + 64 b + j]
+  int h, nq;
+  int qw[OZG_MAXQ], qdt[OZG_MAXQ];  // widths and dtypes (GPU_MV_*) of the Q blocks
+  long n;
+  double* partial;  // [tile][cta][128][64]
+  int* err;
+};
+
+static __device__ __forceinline__ int ozg_col_kind(const ozg_params& prm, int b, int j, const void** ptr)
+{
+  // 0: absent, 1: FP32, 2: FP64
+  if (j < 64) {
+    if (j >= prm.h) return 0;
+    *ptr = prm.cols.col[j];
+    return 2;
+  }
+  const int q = j - 64;
+  if (b >= prm.nq || q >= prm.qw[b]) return 0;
+  *ptr = prm.cols.col[64 + 64 * b + q];
+  return prm.qdt[b] == GPU_MV_FLOAT64 ? 2 : 1;
+}
+
+__global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_constant__ ozg_params prm)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* raws = smem;                  // [2][128 columns][528 B]
+  unsigned char* adig = smem + 2 * OZG_RAW;    // [S][128 rows][128 B]
+  __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag, never_flag;
+  __shared__ int part[1024];       // per (column, 8-row group) largest exponent
+  __shared__ int cexp[4][128];     // chunk scales, by chunk modulo 4
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int b = blockIdx.y;
+  const long nchunks = (prm.n + OZG_ROWS - 1) / OZG_ROWS;
+  const long my_chunks = (long)blockIdx.x < nchunks ? (nchunks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+
+  if (tid == 0) {
+    abort_flag = 0;
+    never_flag = 0;
+    for (int s = 0; s < 2; s++) {
+      mbar_init(&raw_full[s], 1);
+      mbar_init(&raw_empty[s], OZG_NPROD);
+      mbar_init(&acc_full[s], 1);
+      mbar_init(&acc_empty[s], 256);
+    }
+    mbar_init(&a_full, OZG_NPROD);
+    mbar_init(&a_empty, 1);
+    mbar_init(&done_bar, 1);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(512u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 1) {
+    // ------------------------------------------------------- bulk copies
+    long issued[2] = {0, 0};  // chunks issued per slot
+    for (long c = 0; c < my_chunks; c++) {
+      const int slot = (int)(c & 1);
+      int stop = 0;
+      if (lane == 0) {
+        if (c >= 2 && !mbar_wait(&raw_empty[slot], (uint32_t)(((c >> 1) - 1) & 1), &abort_flag)) {
+          abort_flag = 1;
+          atomicExch(prm.err, 21);
+        }
+        stop = abort_flag;
+      }
+      if (__shfl_sync(0xffffffffu, stop, 0)) break;
+      const long r0 = (blockIdx.x + c * gridDim.x) * OZG_ROWS;
+      const long rows = min((long)OZG_ROWS, prm.n - r0);
+      // every column's copy covers whole 16-byte pieces
+      const uint32_t b8 = (uint32_t)(((rows + 1) & ~1L) * 8), b4 = (uint32_t)(((rows + 3) & ~3L) * 4);
+      uint32_t total = 0;
+      for (int j = 0; j < 128; j++) {
+        const void* ptr;
+        const int kind = ozg_col_kind(prm, b, j, &ptr);
+        total += kind == 2 ? b8 : (kind == 1 ? b4 : 0u);
+      }
+      if (lane == 0) mbar_expect_tx(&raw_full[slot], total);
+      __syncwarp();
+      unsigned char* raw = raws + slot * OZG_RAW;
+      for (int j = lane; j < 128; j += 32) {
+        const void* ptr;
+        const int kind = ozg_col_kind(prm, b, j, &ptr);
+        if (kind == 2)
+          bulk_g2s(raw + j * OZG_COLSTRIDE, (const double*)ptr + r0, b8, &raw_full[slot]);
+        else if (kind == 1)
+          bulk_g2s(raw + j * OZG_COLSTRIDE, (const float*)ptr + r0, b4, &raw_full[slot]);
+      }
+      issued[slot] = c + 1;
+    }
+    // no copy may still be landing when the CTA exits
+    for (int s = 0; s < 2; s++)
+      if (issued[s] > 0) mbar_wait(&raw_full[s], (uint32_t)(((issued[s] - 1) >> 1) & 1), &never_flag);
+  } else if (warp == 2 || warp == 3 || warp >= 12) {
+    // ------------------------------------------------------- digit slices
+    // (every producer runs every iteration: the named barrier below must be
+    // reached by all of them; an abort only skips the work)
+    const int p = (warp < 4 ? warp - 2 : warp - 10) * 32 + lane;
+    for (long c = 0; c < my_chunks; c++) {
+      const int slot = (int)(c & 1);
+      if (!abort_flag && !mbar_wait(&raw_full[slot], (uint32_t)((c >> 1) & 1), &abort_flag)) {
+        abort_flag = 1;
+        atomicExch(prm.err, 22);
+      }
+      const long r0 = (blockIdx.x + c * gridDim.x) * OZG_ROWS;
+      const int rows = (int)min((long)OZG_ROWS, prm.n - r0);
+      const unsigned char* raw = raws + slot * OZG_RAW;
+      // pass 1: largest exponent of each (column, 8-row group)
+      for (int u = p; u < 1024; u += OZG_NPROD) {
+        const int j = u >> 3, q = u & 7;
+        const void* ptr;
+        const int kind = abort_flag ? 0 : ozg_col_kind(prm, b, j, &ptr);
+        int e = 0;
+        for (int k = 0; k < 8 && kind; k++) {
+          const int rr = 8 * q + k;
+          if (rr >= rows) break;
+          e = max(e, kind == 2 ? oz_bexp64(((const double*)(raw + j * OZG_COLSTRIDE))[rr])
+                               : oz_bexp32(((const float*)(raw + j * OZG_COLSTRIDE))[rr]));
+        }
+        part[u] = e;
+      }
+      named_bar(1, OZG_NPROD);
+      // the digit slices are free once the previous chunk's MMAs completed
+      if (c >= 1 && !abort_flag && !mbar_wait(&a_empty, (uint32_t)((c - 1) & 1), &abort_flag)) {
+        abort_flag = 1;
+        atomicExch(prm.err, 23);
+      }
+      if (!abort_flag) {
+        tc_fence_after();
+        // pass 2: the digits of (column j, rows 8q .. 8q + 7)
+        for (int u = p; u < 1024; u += OZG_NPROD) {
+          const int j = u >> 3, q = u & 7;
+          int E = 0;
+#pragma unroll
+          for (int g = 0; g < 8; g++) E = max(E, part[8 * j + g]);
+          const void* ptr;
+          const int kind = ozg_col_kind(prm, b, j, &ptr);
+          uint32_t pk[OZG_S][4];
+#pragma unroll
+          for (int k = 0; k < 8; k += 2) {
+            uint32_t d0[OZG_S], d1[OZG_S];
+#pragma unroll
+            for (int x = 0; x < 2; x++) {
+              const int rr = 8 * q + k + x;
+              uint64_t U = 0;
+              uint32_t neg = 0;
+              if (kind == 2 && rr < rows) {
+                const double v = ((const double*)(raw + j * OZG_COLSTRIDE))[rr];
+                U = oz_fixed64<OZG_F>(v, E);
+                neg = (uint32_t)((uint64_t)__double_as_longlong(v) >> 63);
+              } else if (kind == 1 && rr < rows) {
+                const float v = ((const float*)(raw + j * OZG_COLSTRIDE))[rr];
+                U = oz_fixed32<OZG_F>(v, E);
+                neg = __float_as_uint(v) >> 31;
+              }
+              if (x == 0)
+                oz_digits<OZG_S>(U, neg, d0);
+              else
+                oz_digits<OZG_S>(U, neg, d1);
+            }
+#pragma unroll
+            for (int t = 0; t < OZG_S; t++) pk[t][k >> 1] = d0[t] | (d1[t] << 16);
+          }
+          const uint32_t off = (uint32_t)j * 128u + ((uint32_t)(q ^ (j & 7)) << 4);
+#pragma unroll
+          for (int t = 0; t < OZG_S; t++)
+            *(uint4*)(adig + t * OZG_SLICE + off) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+          if (q == 0) cexp[c & 3][j] = kind ? E : 0;
+        }
+        fence_proxy_async();
+        mbar_arrive(&a_full);
+        mbar_arrive(&raw_empty[slot]);
+      }
+      named_bar(1, OZG_NPROD);  // part[] is rewritten by the next chunk's pass 1
+    }
+  } else if (warp == 0 && lane == 0) {
+    // ------------------------------------------------------- MMA issuer
+    const uint32_t idesc = bf16_idesc(128, 64);
+    const uint32_t abase = smem_u32(adig);
+    for (long c = 0; c < my_chunks && !abort_flag; c++) {
+      const int buf = (int)(c & 1);
+      if (!mbar_wait(&a_full, (uint32_t)(c & 1), &abort_flag)) {
+        abort_flag = 1;
+        atomicExch(prm.err, 24);
+        break;
+      }
+      if (c >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((c >> 1) - 1) & 1), &abort_flag)) {
+        abort_flag = 1;
+        atomicExch(prm.err, 25);
+        break;
+      }
+      tc_fence_after();
+      for (int t = 0; t < OZG_S; t++)
+        for (int u = 0; u + t < OZG_S; u++) {
+          const uint32_t d = tmem + (uint32_t)(buf * 256 + (t + u) * 64);
+          for (int ks = 0; ks < 4; ks++)
+            mma_bf16(d, sw128_desc(abase + t * OZG_SLICE + ks * 32), sw128_desc(abase + u * OZG_SLICE + ks * 32),
+                     idesc, (t > 0 || ks > 0) ? 1u : 0u);
+        }
+      mma_commit(&a_empty);
+      mma_commit(&acc_full[buf]);
+    }
+    mma_commit(&done_bar);
+  } else if (warp >= 4 && warp < 12) {
+    // ------------------------------------------------------- epilogue
+    const int quarter = warp & 3, ihalf = (warp - 4) >> 2;
+    const int j = 32 * quarter + lane;
+    float hi[32], lo[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) hi[i] = lo[i] = 0.f;
+    bool ok = true;
+    for (long c = 0; c < my_chunks; c++) {
+      const int buf = (int)(c & 1);
+      const bool got = mbar_wait(&acc_full[buf], (uint32_t)((c >> 1) & 1), &abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {  // tcgen05.ld needs the whole warp
+        abort_flag = 1;
+        atomicExch(prm.err, 26);
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const int* ce = cexp[c & 3];
+      const int ej = ce[j];
+      // 2^(E - 1022 - 7) per factor: the digit sums carry 2^-7 per factor
+      const float fj = (ej >= 903 && ej <= 1156) ? __uint_as_float((uint32_t)(ej - 1029 + 127) << 23) : 0.f;
+      const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(buf * 256 + 32 * ihalf);
+#pragma unroll
+      for (int g = 0; g < 4; g++) {
+        // Horner over the levels, highest first: v = sum_L S_L 2^(-7 L)
+        float v[8];
+#pragma unroll
+        for (int L = OZG_S - 1; L >= 0; L--) {
+          uint32_t r[8];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                "=r"(r[7])
+              : "r"(tl + (uint32_t)(L * 64 + 8 * g)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int x = 0; x < 8; x++)
+            v[x] = (L == OZG_S - 1) ? __uint_as_float(r[x]) : fmaf(v[x], 0.0078125f, __uint_as_float(r[x]));
+        }
+#pragma unroll
+        for (int x = 0; x < 8; x++) {
+          const int ii = 8 * g + x;
+          const int ei = ce[32 * ihalf + ii];
+          const float fi = (ei >= 903 && ei <= 1156) ? __uint_as_float((uint32_t)(ei - 1029 + 127) << 23) : 0.f;
+          const float y = v[x] * fj * fi;
+          // two-sum: hi + y = sum + err exactly
+          const float sum = hi[ii] + y;
+          const float bv = sum - hi[ii];
+          const float err = (hi[ii] - (sum - bv)) + (y - bv);
+          hi[ii] = sum;
+          lo[ii] += err;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+    double* out = prm.partial + ((size_t)b * gridDim.x + blockIdx.x) * 128 * 64 + (size_t)j * 64 + 32 * ihalf;
+#pragma unroll
+    for (int i = 0; i < 32; i++) out[i] = ok ? (double)hi[i] + (double)lo[i] : 0.0;
+  }
+  // TMEM is freed only after the last MMA has completed and every epilogue
+  // read has finished
+  if (warp == 0) {
+    mbar_wait(&done_bar, 0, &never_flag);
+    __syncwarp();
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+  }
+}
+
+// G(i, col) for i < h: col < h -> tile 0, operand row col; col in Q_b's
+// range -> tile b, operand row 64 + (col - start of Q_b); CTAs summed in order
+struct ozg_offsets {
+  int q[OZG_MAXQ + 1];
+};
+
+__global__ void oz_gram_reduce_kernel(const double* __restrict__ partial, int gx, int h, int nq,
+                                      ozg_offsets qoff, int wtot, double* G, int ldg, const int* err)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= h * wtot) return;
+  const int i = e % h, col = e / h;
+  int tile = 0, row = col;
+  if (col >= h) {
+    for (int q = 0; q < nq; q++)
+      if (col >= qoff.q[q] && col < qoff.q[q + 1]) {
+        tile = q;
+        row = 64 + col - qoff.q[q];
+      }
+  }
+  double s = 0.0;
+  const double* p = partial + (size_t)tile * gx * 8192 + (size_t)row * 64 + i;
+  for (int x = 0; x < gx; x++) s += p[(size_t)x * 8192];
+  if (*err) s = __longlong_as_double(0x7ff8000000000000LL);  // NaN: the caller sees a failed Gram
+  G[i + (size_t)col * ldg] = s;
+}
+
+extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int nq, const blk_cols* Q,
+                          const int* qw, const int* qdt, double* G, int ldg)
+{
+  if (h < 1 || h > 64 || nq < 0 || nq > OZG_MAXQ || n <= 0)
+    return gb_fail(ctx, "oz_gram: shape (h %d, %d blocks) not supported", h, nq);
+  ozg_params prm;
+  memset(&prm, 0, sizeof(prm));
+  prm.h = h;
+  prm.nq = nq;
+  prm.n = n;
+  for (int c = 0; c < h; c++) {
+    prm.cols.col[c] = L->col[c];
+    if ((uintptr_t)L->col[c] & 15) return gb_fail(ctx, "oz_gram: column %d of L not 16-byte aligned", c);
+  }
+  int wtot = h;
+  ozg_offsets qoff;
+  for (int q = 0; q < nq; q++) {
+    if (qw[q] < 0 || qw[q] > 64) return gb_fail(ctx, "oz_gram: block %d has %d columns", q, qw[q]);
+    prm.qw[q] = qw[q];
+    prm.qdt[q] = qdt[q];
+    qoff.q[q] = wtot;
+    for (int j = 0; j < qw[q]; j++) {
+      prm.cols.col[64 + 64 * q + j] = Q[q].col[j];
+      if ((uintptr_t)Q[q].col[j] & 15)
+        return gb_fail(ctx, "oz_gram: column %d of block %d not 16-byte aligned", j, q);
+    }
+    wtot += qw[q];
+  }
+  qoff.q[nq] = wtot;
+  const int ntiles = nq > 0 ? nq : 1;
+  const long nchunks = (n + OZG_ROWS - 1) / OZG_ROWS;
+  long gx = ctx->num_sms / ntiles;
+  if (gx < 1) gx = 1;
+  if (gx > nchunks) gx = nchunks;
+  const size_t pbytes = sizeof(double) * (size_t)ntiles * gx * 8192;
+  char* ws = (char*)gb_workspace(ctx, pbytes + 256);
+  if (!ws) return -1;
+  prm.partial = (double*)ws;
+  prm.err = (int*)(ws + pbytes);
+  if (cudaMemsetAsync(prm.err, 0, sizeof(int), (cudaStream_t)ctx->stream) != cudaSuccess)
+    return gb_fail(ctx, "oz_gram: memset failed");
+  if (cudaFuncSetAttribute(oz_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZG_SMEM) !=
+      cudaSuccess)
+    return gb_fail(ctx, "oz_gram: cannot reserve %d bytes of shared memory", OZG_SMEM);
+  gb_prof_rec pr;
+  gb_prof_begin(ctx, &pr, GB_K_OZ_GRAM);
+  oz_gram_kernel<<<dim3((unsigned)gx, (unsigned)ntiles), OZG_THREADS, OZG_SMEM, (cudaStream_t)ctx->stream>>>(prm);
+  int rc = gb_cuda_check(ctx, (int)cudaGetLastError(), "oz_gram");
+  if (rc) return rc;
+  oz_gram_reduce_kernel<<<(h * wtot + 255) / 256, 256, 0, (cudaStream_t)ctx->stream>>>(
+      prm.partial, (int)gx, h, nq, qoff, wtot, G, ldg, prm.err);
+  double bytes = 8.0 * n * h;
+  for (int q = 0; q < nq; q++) bytes += (qdt[q] == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * qw[q];
+  gb_prof_end(ctx, &pr, bytes, 2.0 * n * h * wtot);
+  gb_count_launch(2);
+  return gb_cuda_check(ctx, (int)cudaGetLastError(), "oz_gram_reduce");
+}
+
+// ------------------------------------------------------- C-ABI entry point
+extern "C" int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, double* G_host, int ldg)
+{
+  gpu_Context* ctx = L->ctx;
+  const int h = L->num_active;
+  if (L->dtype != GPU_MV_FLOAT64) return gb_fail(ctx, "SplitGram: L must be FP64");
+  if (nq < 0 || nq > OZG_MAXQ) return gb_fail(ctx, "SplitGram: at most %d Q blocks", OZG_MAXQ);
+  blk_cols cl;
+  blk_cols* cq = (blk_cols*)malloc(sizeof(blk_cols) * (nq > 0 ? nq : 1));
+  int qw[OZG_MAXQ], qdt[OZG_MAXQ];
+  int wtot = h;
+  if (!cq) return gb_fail(ctx, "SplitGram: out of host memory");
+  gb_mv_fill_cols(L, &cl, 0);
+  for (int q = 0; q < nq; q++) {
+    if (Q[q]->size != L->size) {
+      free(cq);
+      return gb_fail(ctx, "SplitGram: block %d has %ld rows, L has %ld", q, Q[q]->size, L->size);
+    }
+    gb_mv_fill_cols(Q[q], &cq[q], 0);
+    qw[q] = Q[q]->num_active;
+    qdt[q] = Q[q]->dtype;
+    wtot += qw[q];
+  }
+  if (ldg < h) {
+    free(cq);
+    return gb_fail(ctx, "SplitGram: ldg < h");
+  }
+  double* d = (double*)gb_device_alloc(ctx, sizeof(double) * (size_t)h * wtot);
+  int rc = d ? 0 : -1;
+  if (!rc) rc = gb_oz_gram(ctx, L->size, &cl, h, nq, cq, qw, qdt, d, h);
+  double* hbuf = (double*)malloc(sizeof(double) * (size_t)h * wtot);
+  if (!rc && !hbuf) rc = gb_fail(ctx, "SplitGram: out of host memory");
+  if (!rc) rc = gb_memcpy_d2h(ctx, hbuf, d, sizeof(double) * (size_t)h * wtot);
+  if (!rc)
+    for (int j = 0; j < wtot; j++)
+      for (int i = 0; i < h; i++) G_host[i + (size_t)j * ldg] = hbuf[i + (size_t)j * h];
+  free(hbuf);
+  free(cq);
+  gb_sync(ctx);
+  gb_device_free(d);
+  return rc;
+}

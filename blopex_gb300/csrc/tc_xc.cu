@@ -334,8 +334,12 @@ extern "C" int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc
   const int h = X->num_active, w = Y->num_active;
   if (ldc < h) return gb_fail(ctx, "BlockUpdate: ldc < h");
   if (Z && Z->num_active != w) return gb_fail(ctx, "BlockUpdate: Z width differs from Y");
-  if (X->dtype != Y->dtype || (Z && Z->dtype != Y->dtype))
+  if (mode == 2) {
+    if (X->dtype != GPU_MV_FLOAT64 || Y->dtype != GPU_MV_FLOAT64)
+      return gb_fail(ctx, "BlockUpdate: mode 2 needs FP64 X and Y");
+  } else if (X->dtype != Y->dtype || (Z && Z->dtype != Y->dtype)) {
     return gb_fail(ctx, "BlockUpdate: mixed precisions");
+  }
   if (mode == 1 && X->dtype != GPU_MV_FLOAT32) return gb_fail(ctx, "BlockUpdate: mode 1 needs FP32 blocks");
   if (h == 0 || w == 0) return 0;
   blk_cols cx, cy, cz;
@@ -348,8 +352,10 @@ extern "C" int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc
   if (!rc) {
     if (mode == 0)
       rc = gb_bymat(ctx, X->dtype, X->size, &cx, h, C, ldc, &cy, w, Z ? &cz : NULL);
-    else
+    else if (mode == 1)
       rc = gb_tc_xc(ctx, X->size, &cx, h, C, ldc, &cy, w, Z ? &cz : NULL);
+    else
+      rc = gb_oz_xc(ctx, X->size, &cx, h, C, ldc, &cy, w, Z ? &cz : NULL, Z ? Z->dtype : 0, NULL);
   }
   int err = 0;
   if (!rc) rc = gb_device_error(ctx, &err);

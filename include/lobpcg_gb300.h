@@ -207,9 +207,21 @@ int gpu_ExplicitGram(gpu_MultiVector* X, gpu_MultiVector* R, gpu_MultiVector* P,
    (blopex_serial_double/multivector/multi_vector.c:474-524) with the fused
    accumulate of the solver's X update.  mode 0: CUDA-core kernel (FP64 or FP32
    blocks); mode 1: tensor cores, compensated 3xTF32 (FP32 blocks, h <= 128,
-   w <= 64, 16-byte aligned columns).  Z may be NULL. */
+   w <= 64, 16-byte aligned columns); mode 2: tensor cores, FP64-accurate
+   products by error-free splitting into bf16 digits (FP64 X and Y, h <= 64,
+   w <= 64; Z FP32 or FP64).  Z may be NULL. */
 int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_MultiVector* Y,
                     gpu_MultiVector* Z, int mode);
+
+/* G = L' [L Q_0 .. Q_{nq-1}] over the active columns, FP64-accurate on the
+   tensor cores (error-free splitting of 64-row chunks into bf16 digits,
+   exact FP32 accumulation per chunk, unbiased sums across chunks): L FP64
+   with at most 64 active columns, each Q_b FP32 or FP64 with at most 64
+   (nq <= 4).  G_host (h x (h + sum of the Q widths), leading dimension ldg)
+   receives L'L and then each L'Q_b.  The X rows of the reference's gramB
+   (serial_Multi_VectorInnerProd, multi_vector.c:354-406, at lobpcg.c:
+   1105-1160) as the mixed mode forms them. */
+int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, double* G_host, int ldg);
 
 /* ---------------------------------------------------------------- */
 /* External problems: the reference tools' file formats                */

@@ -130,6 +130,19 @@ def build(name: str) -> Case:
         return Case(name, "Laplacian 8^3, k=4: the 4th Rayleigh-Ritz solve reports failure "
                     "(lobpcg.c:1167-1176)", 512, 4, 9, 1e-8, 1e-50, 60,
                     csr=P.laplacian3d_csr(8, 8, 8), sygv_fail_at=4)
+    if name == "lap128_k32_jacobi_it30":
+        n = 128 ** 3
+        return Case(name, "the 128^3 plain-FP64 configuration for its first 30 iterations: 7-point "
+                    "Laplacian 128^3 CSR (n=2097152), k=32, Jacobi T = 1/diag(A) = I/6, X0 seed 1, "
+                    "tol 1e-8, maxit 30", n, 32, 1, 1e-8, 1e-50, 30,
+                    csr=P.laplacian3d_csr(128, 128, 128), t_diag=np.full(n, 1.0 / 6.0))
+    if name == "st7vc128_k64_jacobi_it20":
+        cx, cy, cz = P.stencil7_coefficients(128, 128, 128, seed=2)
+        return Case(name, "the variable-coefficient stencil configuration at 128^3 for its first "
+                    "20 iterations: faces exp(N(0,1)) seed 2 (assembled as CSR), k=64, Jacobi T, "
+                    "X0 seed 2, tol 1e-8, maxit 20", 128 ** 3, 64, 2, 1e-8, 1e-50, 20,
+                    csr=P.stencil7_to_csr(cx, cy, cz),
+                    t_diag=1.0 / P.stencil7_diagonal(cx, cy, cz))
     raise KeyError(name)
 
 
@@ -137,3 +150,8 @@ NAMES = ["serial_driver", "serial_driver_v1", "lap20_k10", "lap20_k10_maxit1000"
          "st7vc_12_k6_jacobi", "gen27_8_k4", "constraints_diag40", "all_paths_lap6",
          "lap10_k1", "bad_initial_block", "wrong_constraints",
          "fail_p_orth", "fail_r_orth", "fail_gevp"]
+
+# Cases at the benchmark sizes (128^3): each reference run takes tens of
+# minutes on one core, so they are generated separately (make_golden.py
+# --large) and replayed only by the GPU tests.
+LARGE_NAMES = ["lap128_k32_jacobi_it30", "st7vc128_k64_jacobi_it20"]

@@ -7,8 +7,12 @@ inputs and records exit flag, iteration count, eigenvalues, residual norms
 and their histories.  Inputs are rebuilt by the tests from the same
 generators; a SHA-256 of every input array is stored to pin them.
 
-Run in a container that has the reference checkout:
-    python tests/golden/make_golden.py
+Run in a container that has the reference checkout (its location in the
+environment variable BLOPEX_REFERENCE_DIR):
+    python tests/golden/make_golden.py            # the small cases
+    python tests/golden/make_golden.py --large    # the 128^3 cases (hours
+                                                  # of CPU; the three builds
+                                                  # run in parallel processes)
 """
 from __future__ import annotations
 
@@ -85,10 +89,59 @@ def run_case(name: str) -> dict:
     return out
 
 
+def _large_variant(name: str, variant: str) -> dict:
+    """One reference build on one large case (runs in a spawned process)."""
+    import time
+
+    case = C.build(name)
+    kw = dict(seed=case.seed, atol=case.atol, rtol=case.rtol, maxit=case.maxit,
+              t_diag=case.t_diag, b_diag=case.b_diag, csr_arrays=case.csr)
+    t0 = time.time()
+    r = O.ref_solve(case.n, case.k, variant=variant, **kw)
+    ncol = r.iterations + 1
+    return {"flag": r.flag, "iterations": r.iterations, "lambda": r.lam.tolist(),
+            "resnorm": r.res.tolist(), "lambda_hist": r.lam_hist[:, :ncol].T.tolist(),
+            "res_hist": r.res_hist[:, :ncol].T.tolist(), "seconds": time.time() - t0}
+
+
+def main_large(names):
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    jobs = {}
+    with ProcessPoolExecutor(max_workers=3 * len(names),
+                             mp_context=mp.get_context("spawn")) as ex:
+        for name in names:
+            for v in ("", "fma", "x87"):
+                jobs[(name, v)] = ex.submit(_large_variant, name, v)
+        for name in names:
+            case = C.build(name)
+            plain = jobs[(name, "")].result()
+            out = {"name": name, "description": case.description, "n": case.n, "k": case.k,
+                   "atol": case.atol, "rtol": case.rtol, "maxit": case.maxit}
+            out.update({key: plain[key] for key in ("flag", "iterations", "lambda", "resnorm",
+                                                      "lambda_hist", "res_hist")})
+            out["reference_seconds_one_core"] = plain["seconds"]
+            out["inputs_sha256"] = {key: sha(val) for key, val in case.arrays().items()}
+            out["variants"] = {}
+            for v in ("fma", "x87"):
+                rv = jobs[(name, v)].result()
+                out["variants"][v] = {key: rv[key] for key in
+                                      ("flag", "iterations", "lambda", "resnorm",
+                                       "lambda_hist", "res_hist")}
+            with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+                json.dump(out, f, indent=0)
+            print(f"{name}: flag {out['flag']} iterations {out['iterations']} "
+                  f"({plain['seconds']:.0f} s)", flush=True)
+
+
 def main():
     if not O.have_ref():
         O.build(ref=True)
     O.build_ref_variants()
+    if "--large" in sys.argv:
+        main_large(C.LARGE_NAMES)
+        return
     for name in C.NAMES:
         g = run_case(name)
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:
