@@ -30,7 +30,7 @@ class Options(ctypes.Structure):
                 ("sygv_fail_at", c_int), ("explicit_pivot_below", c_double),
                 ("fp32_accurate_op", c_int), ("recompute_ap", c_int), ("explicit_fp64", c_int),
                 ("accum64", c_int),
-                ("rr_method", c_int), ("fp32_precond", c_int)]
+                ("rr_method", c_int), ("fp32_precond", c_int), ("split_products", c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -40,7 +40,9 @@ class Stats(ctypes.Structure):
                 ("seconds_fp64", c_double), ("final_max_residual", c_double),
                 ("rr_calls", c_int), ("rr_jacobi32_sweeps", c_int), ("rr_max_cluster", c_int),
                 ("rr_fallbacks", c_int), ("rr_graded", c_int),
-                ("explicit_undos", c_int), ("explicit_p_drops", c_int)]
+                ("explicit_undos", c_int), ("explicit_p_drops", c_int),
+                ("iterations_split", c_int), ("handover_reason", c_int),
+                ("device_errors", c_int)]
 
 
 class KernelTime(ctypes.Structure):

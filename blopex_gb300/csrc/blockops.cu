@@ -612,6 +612,67 @@ extern "C" int gb_accumulate64(gpu_Context* ctx, long n, const blk_cols* X64, co
   return CUDA_LAUNCH_CHECK(ctx, "accumulate64");
 }
 
+// The explicit pencil (G, H) of [X R P] from the exact Gram products of the
+// split mode.  Inputs (column-major FP64):
+//   Hx = X'[X R P]          (k x m, ld k)
+//   Hr = R'[R P AR AP]      (nR x (2 nR + 2 nP), ld nR)
+//   Hp = P'[P AP]           (nP x 2 nP, ld nP)
+//   Gr = RS'[RS X R P]      (k x (k + m), ld k), RS = lambda X - A X
+// with lambda the Rayleigh quotients of X.  The X rows of G are formed in
+// residual form, G(i, c) = X_i' A S_c = lambda_i X_i' S_c - RS_i' S_c, so that
+// A X (whose norm is the spectrum's scale) never enters a product; the other
+// blocks are R'AR, R'AP, P'AP.  Symmetric blocks are averaged with their
+// transposes.
+__global__ void split_pencil_kernel(const double* __restrict__ Hx, const double* __restrict__ Hr,
+                                    const double* __restrict__ Hp, const double* __restrict__ Gr,
+                                    double* G, double* H, int ld, const double* __restrict__ lam,
+                                    int k, int nR, int nP)
+{
+  const int m = k + nR + nP;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * m) return;
+  const int a = e % m, b = e / m;
+  double g, h;
+  if (a < k || b < k) {
+    if (a < k && b < k) {
+      const double h1 = Hx[a + (size_t)b * k], h2 = Hx[b + (size_t)a * k];
+      h = 0.5 * (h1 + h2);
+      g = 0.5 * ((lam[a] * h1 - Gr[a + (size_t)(k + b) * k]) + (lam[b] * h2 - Gr[b + (size_t)(k + a) * k]));
+    } else {
+      const int i = a < k ? a : b, c = a < k ? b : a;
+      h = Hx[i + (size_t)c * k];
+      g = lam[i] * h - Gr[i + (size_t)(k + c) * k];
+    }
+  } else {
+    const int ra = a - k, rb = b - k;  // offsets in [R P]
+    if (ra < nR && rb < nR) {
+      h = 0.5 * (Hr[ra + (size_t)rb * nR] + Hr[rb + (size_t)ra * nR]);
+      const size_t o = (size_t)(nR + nP) * nR;
+      g = 0.5 * (Hr[o + ra + (size_t)rb * nR] + Hr[o + rb + (size_t)ra * nR]);
+    } else if (ra < nR || rb < nR) {
+      const int r = ra < nR ? ra : rb, p = (ra < nR ? rb : ra) - nR;
+      h = Hr[r + (size_t)(nR + p) * nR];
+      g = Hr[r + (size_t)(2 * nR + nP + p) * nR];
+    } else {
+      const int pa = ra - nR, pb = rb - nR;
+      h = 0.5 * (Hp[pa + (size_t)pb * nP] + Hp[pb + (size_t)pa * nP]);
+      g = 0.5 * (Hp[pa + (size_t)(nP + pb) * nP] + Hp[pb + (size_t)(nP + pa) * nP]);
+    }
+  }
+  G[a + (size_t)b * ld] = g;
+  H[a + (size_t)b * ld] = h;
+}
+
+extern "C" int gb_split_pencil(gpu_Context* ctx, const double* Hx, const double* Hr, const double* Hp,
+                               const double* Gr, double* G, double* H, int ld, const double* lam, int k,
+                               int nR, int nP)
+{
+  const int m = k + nR + nP;
+  split_pencil_kernel<<<(m * m + 255) / 256, 256, 0, S(ctx)>>>(Hx, Hr, Hp, Gr, G, H, ld, lam, k, nR, nP);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "split pencil");
+}
+
 __global__ void rayleigh_kernel(int w, const double* num, const double* den, double* lam)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -770,9 +831,13 @@ static int gram_noalloc_launch(long n, const blk_cols* X, int h, const blk_cols*
   splits = (n + rows - 1) / rows;
   if (splits < 1) splits = 1;
   dim3 grid(gx, gy, (unsigned)splits);
+  // an error left pending by earlier work on this thread is not ours to
+  // clear: report it (-3) and leave it for its owner to read
+  if (cudaPeekAtLastError() != cudaSuccess) return -3;
   // every partial element of the used splits is written before the
   // reduction reads it, so stale contents from an earlier call never leak
   gram_partial_kernel<T, TM, TN><<<grid, 256, 0, stream>>>(*X, h, *Y, w, n, rows, partial);
+  if (cudaGetLastError() != cudaSuccess) return -3;
   gram_reduce_kernel<<<(h * w + 255) / 256, 256, 0, stream>>>(partial, (int)splits, h, w, G, ldg);
   gb_count_launch(2);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;

@@ -65,6 +65,7 @@ static void default_options(lobpcg_gpu_options* o)
   o->explicit_pivot_below = 1e-6;
   o->fp32_stall = 20;
   o->tensor_cores = 1;
+  o->split_products = 1;
 }
 
 extern "C" gpu_Context* gpu_ContextCreate(int device, void* stream)

@@ -153,6 +153,13 @@ int gb_chol_deflate(gpu_Context* ctx, double* A, int ld, int m, double tol, int*
    the kx smallest eigenvalues) */
 int gb_deflate_pencil(gpu_Context* ctx, double* G, double* H, int ld, int mtot, int off, int m,
                       const int* dropped, int kx);
+/* the explicit pencil (G, H; m x m, m = k + nR + nP, leading dimension ld)
+   of the split mode from Hx = X'[X R P] (ld k), Hr = R'[R P AR AP] (ld nR),
+   Hp = P'[P AP] (ld nP), Gr = RS'[RS X R P] (ld k; RS = lambda X - A X) and
+   lambda: the X rows of G in residual form, lambda_i X_i'S_c - RS_i'S_c */
+int gb_split_pencil(gpu_Context* ctx, const double* Hx, const double* Hr, const double* Hp,
+                    const double* Gr, double* G, double* H, int ld, const double* lam, int k,
+                    int nR, int nP);
 /* A(i,i) += alpha for i < m (device small matrix) */
 int gb_small_add_diag(gpu_Context* ctx, double* A, int ld, int m, double alpha);
 /* drand48-compatible fill of column-major storage, columns listed in idx */
@@ -178,12 +185,12 @@ int gb_tc_xc(gpu_Context* ctx, long n, const blk_cols* X, int h, const double* C
 int gb_oz_xc(gpu_Context* ctx, long n, const blk_cols* X, int h, const double* C, int ldc,
              const blk_cols* Y, int w, const blk_cols* Z, int z_dtype, const blk_cols* Y32);
 /* FP64-accurate Gram G = L' [L Q_0 Q_1 ...] on the tensor cores (oz_gram.cu):
-   L an FP64 block of h <= 64 columns; nq blocks Q_b of up to 64 columns each,
-   FP32 or FP64 (qdt[b]); every column 16-byte aligned and readable up to a
-   row count rounded to 4.  G (FP64 device, ldg) receives L'L in columns 0..h
-   and L'Q_b in the following columns, in order. */
-int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int nq, const blk_cols* Q,
-               const int* qw, const int* qdt, double* G, int ldg);
+   L a block of h <= 64 columns, FP32 or FP64 (ldt); nq <= 4 blocks Q_b of up
+   to 64 columns each, FP32 or FP64 (qdt[b]); every column 16-byte aligned and
+   readable up to a row count rounded to 4.  G (FP64 device, ldg) receives L'L
+   in columns 0..h and L'Q_b in the following columns, in order. */
+int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int ldt, int nq,
+               const blk_cols* Q, const int* qw, const int* qdt, double* G, int ldg);
 /* device error word of the tensor-core kernels (0 = none); clears it */
 int gb_device_error(gpu_Context* ctx, int* err);
 

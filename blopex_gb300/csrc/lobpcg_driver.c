@@ -579,6 +579,8 @@ static int phase_loop(solver_t* s, phase_ctl* ctl)
 
 /* a step whose largest active residual grows by more than this is undone */
 #define EXPLICIT_JUMP 20.0
+/* split mode: consecutive undone steps before the hand-over to FP64 */
+#define SPLIT_MAX_UNDOS 3
 
 static size_t dt_size(int dtype) { return dtype == GPU_MV_FLOAT64 ? 8 : 4; }
 
@@ -607,6 +609,10 @@ typedef struct {
   double* rq;
   int wrote_x64;
   int* pdrop; /* device: P columns dropped by the deflating Cholesky */
+  /* split products (FP64-carried X): RS = lambda X - A X for all k columns
+     (FP32) and Hx = X'[X R P] (FP64, k x 3k) */
+  gpu_MultiVector* RS;
+  double* Hx;
 } explicit_bufs;
 
 /* exact A X in FP64 every this many FP64-accumulated steps (in between, AX is
@@ -673,6 +679,29 @@ static int explicit_residual(solver_t* s, gpu_MultiVector* X, gpu_MultiVector* A
   return 0;
 }
 
+/* split products: RS = lambda X64 - AX64 for all k columns (FP32) and, for
+   the columns listed in act (all when act == NULL), the FP64 residual norms
+   into h_norm */
+static int split_residual(solver_t* s, explicit_bufs* eb, gpu_MultiVector* X64,
+                          gpu_MultiVector* AX64, const int* act, int nact)
+{
+  const int k = s->k;
+  int all[BLK_MAXCOLS];
+  blk_cols x, ax, r;
+  for (int i = 0; i < k; i++) all[i] = i;
+  cols_idx(X64, NULL, k, &x, 0);
+  cols_idx(AX64, NULL, k, &ax, 0);
+  cols_idx(eb->RS, NULL, k, &r, 0);
+  if (gb_residual(s->ctx, GB_RESID_64TO32, s->n, &x, &ax, s->lam, all, &r, k, s->norm2)) return -1;
+  double* tmp = (double*)gb_pinned(s->ctx, sizeof(double) * k);
+  if (!tmp || gb_memcpy_d2h(s->ctx, tmp, s->norm2, sizeof(double) * k)) return -1;
+  if (!act)
+    for (int i = 0; i < k; i++) s->h_norm[i] = sqrt(fabs(tmp[i]));
+  else
+    for (int c = 0; c < nact; c++) s->h_norm[act[c]] = sqrt(fabs(tmp[act[c]]));
+  return 0;
+}
+
 /*
  * The FP32 phase of the mixed mode: block LOBPCG with explicit Gram
  * matrices.  Each iteration forms G = [X R P]'[AX AR AP] and
@@ -713,6 +742,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       tc_ok = 0;
   }
   int comp = 0;
+  int split_undos = 0; /* consecutive undone steps in split mode */
   for (int i = 0; i < k; i++) prev_act[i] = i;  /* phase_setup left R for all columns */
   gb_mv_set_mask_host(X, NULL);
   gb_mv_set_mask_host(AX, NULL);
@@ -726,6 +756,15 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
   gpu_MultiVector *X64 = eb->X64[0], *X64n = eb->X64[1], *AX64 = eb->AX64[0], *AX64n = eb->AX64[1];
   int refresh = 0;
   gpu_MultiVector* t64;
+  /* split products: X and A X carried in FP64 and updated by the FP64-accurate
+     split-operand kernel, the X rows of the pencil FP64-accurate (H from the
+     split-operand Gram, G in residual form); the FP32 products then only
+     shape the corrections, and the phase iterates to the tolerance */
+  const int split = acc64 && eb->RS && eb->Hx && s->ctx->opt.split_products && s->noY;
+  int rs_stale = 0;
+  /* split mode: the FP32 blocks' Grams compensated from the start (TF32
+     products alone make P's Gram block indefinite far more often) */
+  if (split && s->ctx->opt.compensated_below > 0.0) comp = 1;
   if (acc64) {
     gpu_MultiVector* b4[4] = {X64, X64n, AX64, AX64n};
     for (int b = 0; b < 4; b++) gb_mv_set_mask_host(b4[b], NULL);
@@ -738,7 +777,12 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       return -2;
     for (int i = 0; i < k; i++) prev_act[i] = i;
     set_prefix(R, k);
-    if (explicit_residual(s, X64, AX64, X64, prev_act, k)) return -2;
+    if (split) {
+      gb_mv_set_mask_host(eb->RS, NULL);
+      if (split_residual(s, eb, X64, AX64, NULL, k)) return -2;
+    } else if (explicit_residual(s, X64, AX64, X64, prev_act, k)) {
+      return -2;
+    }
   }
 
   for (*it = ctl->it_base + 1; *it <= ctl->maxit; (*it)++) {
@@ -753,8 +797,9 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       double mx = 0.0;
       for (int c = 0; c < nR; c++)
         if (s->h_norm[act[c]] > mx) mx = s->h_norm[act[c]];
-      if (mx < ctl->fp64_below) {
+      if (!split && mx < ctl->fp64_below) {
         ctl->handed_over = 1;
+        s->ctx->stats.handover_reason = 1;
         break;
       }
       /* TF32 products carry ~1e-4 relative errors: compensate once the
@@ -782,12 +827,19 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
           stall = 0;
         } else {
           ctl->handed_over = 1;
+          s->ctx->stats.handover_reason = 2;
           break;
         }
       }
     }
     /* the residual block must hold exactly the active columns */
-    if (nR != prev_nR || memcmp(act, prev_act, sizeof(int) * nR)) {
+    if (split) {
+      if (rs_stale) {
+        /* an undone step left RS with its residual: that of the kept block */
+        if (split_residual(s, eb, X64, AX64, act, 0)) return -2;
+        rs_stale = 0;
+      }
+    } else if (nR != prev_nR || memcmp(act, prev_act, sizeof(int) * nR)) {
       if (acc64 ? explicit_residual(s, X64, AX64, X64, act, nR)
                 : explicit_residual(s, X, AX, BX, act, nR))
         return -2;
@@ -796,7 +848,21 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
     set_prefix(AR, nR);
     set_prefix(s->W, nR);
     if (!s->noB) set_prefix(BR, nR);
-    if (!s->noT) {
+    if (split) {
+      /* R = T (the active columns of RS) */
+      gb_mv_set_mask_host(eb->RS, s->mask);
+      if (!s->noT) {
+        gpu_MultiVector* t;
+        if (d_apply(s, s->T, s->Tdata, eb->RS, s->W)) return -2;
+        t = R;
+        R = s->W;
+        s->W = t;
+        s->R = R;
+      } else if (d_copy(s, eb->RS, R)) {
+        return -2;
+      }
+      gb_mv_set_mask_host(eb->RS, NULL);
+    } else if (!s->noT) {
       gpu_MultiVector* t;
       if (d_apply(s, s->T, s->Tdata, R, s->W)) return -2;
       t = R;
@@ -822,7 +888,40 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       off = cols_idx(AX, NULL, k, &right, 0);
       off = cols_idx(AR, NULL, nR, &right, off);
       cols_idx(AP, act, nP, &right, off);
-      if (tc_ok) {
+      if (split) {
+        /* the whole pencil from exact Grams (split-operand tensor-core
+           products): X'[X R P], R'[R P AR AP], P'[P AP], RS'[RS X R P] */
+        const int F32 = GPU_MV_FLOAT32, F64 = GPU_MV_FLOAT64;
+        const size_t sq = (size_t)k3 * k3;
+        double *Hx = eb->Hx, *Hr = Hx + sq, *Hp = Hr + sq, *Gr = Hp + sq;
+        blk_cols cq[3];
+        int qw[3], qdt[3], nq;
+        blk_cols cl;
+        cols_idx(X64, NULL, k, &cl, 0);
+        nq = 0;
+        cols_idx(R, NULL, nR, &cq[nq], 0), qw[nq] = nR, qdt[nq++] = F32;
+        if (nP) cols_idx(P, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
+        if (gb_oz_gram(s->ctx, s->n, &cl, k, F64, nq, cq, qw, qdt, Hx, k)) return -2;
+        cols_idx(R, NULL, nR, &cl, 0);
+        nq = 0;
+        if (nP) cols_idx(P, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
+        cols_idx(AR, NULL, nR, &cq[nq], 0), qw[nq] = nR, qdt[nq++] = F32;
+        if (nP) cols_idx(AP, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
+        if (gb_oz_gram(s->ctx, s->n, &cl, nR, F32, nq, cq, qw, qdt, Hr, nR)) return -2;
+        if (nP) {
+          cols_idx(P, act, nP, &cl, 0);
+          cols_idx(AP, act, nP, &cq[0], 0), qw[0] = nP, qdt[0] = F32;
+          if (gb_oz_gram(s->ctx, s->n, &cl, nP, F32, 1, cq, qw, qdt, Hp, nP)) return -2;
+        }
+        cols_idx(eb->RS, NULL, k, &cl, 0);
+        nq = 0;
+        cols_idx(X64, NULL, k, &cq[nq], 0), qw[nq] = k, qdt[nq++] = F64;
+        cols_idx(R, NULL, nR, &cq[nq], 0), qw[nq] = nR, qdt[nq++] = F32;
+        if (nP) cols_idx(P, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
+        if (gb_oz_gram(s->ctx, s->n, &cl, k, F32, nq, cq, qw, qdt, Gr, k)) return -2;
+        if (gb_split_pencil(s->ctx, Hx, Hr, Hp, Gr, eb->G, eb->H, k3, s->lam, k, nR, nP)) return -2;
+        s->ctx->stats.iterations_split++;
+      } else if (tc_ok) {
         blk_cols cx, cr, cp, cax, car, cap;
         cols_idx(X, NULL, k, &cx, 0);
         cols_idx(R, NULL, nR, &cr, 0);
@@ -848,7 +947,8 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       int use_p = nP;
       if (explicit_orthonormalise(s, eb, nR, nP, &bad)) return -2;
       if (bad & 3) {
-        ctl->handed_over = 1; /* X or R cannot be orthonormalised in FP32 */
+        ctl->handed_over = 1;
+        s->ctx->stats.handover_reason = 3; /* X or R cannot be orthonormalised in FP32 */
         break;
       }
       if (bad & 4) {
@@ -857,6 +957,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         if (explicit_orthonormalise(s, eb, nR, 0, &bad)) return -2;
         if (bad) {
           ctl->handed_over = 1;
+          s->ctx->stats.handover_reason = 3;
           break;
         }
       }
@@ -877,6 +978,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       }
       if (info != 0 || bad) {
         ctl->handed_over = 1;
+        s->ctx->stats.handover_reason = 4;
         break;
       }
       const int mm = k + nR + use_p;
@@ -889,7 +991,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
 
       /* FP64 accumulation: the FP32 kernels produce the correction
          X (C_X - I) + P, added to the FP64 block below */
-      if (acc64 && gb_small_add_diag(s->ctx, eb->Gs, k3, k, -1.0)) return -2;
+      if (acc64 && !split && gb_small_add_diag(s->ctx, eb->Gs, k3, k, -1.0)) return -2;
       /* P = [R P(act)] C_RP ; X = X C_X + P, and the A / B images */
       const double* cX = eb->Gs;
       const double* cRP = eb->Gs + k;
@@ -904,6 +1006,17 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         cols_idx(srcs[q][2], NULL, k, &y, 0);
         cols_idx(xs[q][0], NULL, k, &xa, 0);
         cols_idx(xs[q][1], NULL, k, &z, 0);
+        if (split) {
+          /* only P and A P here: X and A X follow in FP64 below */
+          if (q == 1 && s->ctx->opt.recompute_ap) {
+            gb_mv_set_mask_host(Pn, NULL);
+            gb_mv_set_mask_host(APn, NULL);
+            if (d_apply(s, s->A, s->Adata, Pn, APn)) return -2;
+          } else if (gb_tc_xc(s->ctx, s->n, &a, h, cRP, k3, &y, k, NULL)) {
+            return -2;
+          }
+          continue;
+        }
         if (q == 1 && s->ctx->opt.recompute_ap) {
           /* A P from P itself: the update [AR AP] C_RP rounds with the
              cancellation between the R and P coefficients (large when R and
@@ -923,7 +1036,32 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
           if (gb_bymat(s->ctx, s->dt, s->n, &xa, k, cX, k3, &z, k, &y)) return -2;
         }
       }
-      if (acc64) {
+      if (split) {
+        /* X = X C_X + P and A X = A X C_X + A P with FP64 accuracy (and the
+           FP32 shadow of X for the next step's tensor-core Grams) */
+        blk_cols x0, x1, z, y32;
+        cols_idx(X64, NULL, k, &x0, 0);
+        cols_idx(X64n, NULL, k, &x1, 0);
+        cols_idx(Pn, NULL, k, &z, 0);
+        cols_idx(Xn, NULL, k, &y32, 0);
+        if (gb_oz_xc(s->ctx, s->n, &x0, k, cX, k3, &x1, k, &z, GPU_MV_FLOAT32, &y32)) return -2;
+        if (++refresh >= ACC64_REFRESH) {
+          /* exact A X: the FP32 A P terms drift from A times P */
+          refresh = 0;
+          if (d_apply(s, s->A, s->Adata, X64n, AX64n)) return -2;
+        } else {
+          cols_idx(AX64, NULL, k, &x0, 0);
+          cols_idx(AX64n, NULL, k, &x1, 0);
+          cols_idx(APn, NULL, k, &z, 0);
+          if (gb_oz_xc(s->ctx, s->n, &x0, k, cX, k3, &x1, k, &z, GPU_MV_FLOAT32, NULL)) return -2;
+        }
+        cols_idx(X64n, NULL, k, &x0, 0);
+        cols_idx(AX64n, NULL, k, &x1, 0);
+        if (gb_rayleigh_quotients(s->ctx, GPU_MV_FLOAT64, s->n, &x0, &x1, k, eb->rq, s->lam))
+          return -2;
+        t64 = X64; X64 = X64n; X64n = t64;
+        t64 = AX64; AX64 = AX64n; AX64n = t64;
+      } else if (acc64) {
         blk_cols x0, xd, x1;
         cols_idx(X64, NULL, k, &x0, 0);
         cols_idx(Xn, NULL, k, &xd, 0);
@@ -974,14 +1112,16 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       int derr = 0;
       if (gb_device_error(s->ctx, &derr)) return -2;
       if (derr) {
+        s->ctx->stats.device_errors++;
         /* a tensor-core kernel gave up waiting: its output is incomplete */
         tc_ok = 0;
         undo = 1;
       }
     }
     if (!undo) {
-      if (acc64 ? explicit_residual(s, X64, AX64, X64, act, nR)
-                : explicit_residual(s, X, AX, BX, act, nR))
+      if (split ? split_residual(s, eb, X64, AX64, act, nR)
+                : acc64 ? explicit_residual(s, X64, AX64, X64, act, nR)
+                        : explicit_residual(s, X, AX, BX, act, nR))
         return -2;
       /* A Ritz pair of the FP32 pencil that is not one of the operator
          (Gram errors ~1e-4 with TF32 products) shows as a jump of the
@@ -1019,16 +1159,25 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       memcpy(s->h_norm, prev_norm, sizeof(double) * k);
       if (gb_memcpy_d2d(s->ctx, s->lam, eb->d, sizeof(double) * k)) return -2;
       s->ctx->stats.explicit_undos++;
-      if (!tc_ok || comp) {
+      if (split && tc_ok && ++split_undos <= SPLIT_MAX_UNDOS) {
+        /* with FP64-accurate X rows a jump is LOBPCG's own (the FP64 path
+           shows them too): retry the step from the kept block without P,
+           the reference's restart (lobpcg.c:1056-1063) taken on purpose */
+        comp = 1;
+        haveP = 0;
+      } else if (!tc_ok || comp) {
         ctl->handed_over = 1;
+        s->ctx->stats.handover_reason = 5;
         break;
       }
       comp = 1;
       stall = 0;
       prev_nR = -1; /* R holds the rejected step's residual: recompute */
+      rs_stale = split;
     } else {
       prev_nR = nR;
       memcpy(prev_act, act, sizeof(int) * nR);
+      split_undos = 0;
     }
     {
       const int col = *it;
@@ -1220,12 +1369,18 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
         eb.G = (double*)gb_device_alloc(ctx, sizeof(double) * (8 * sq + 4 * (size_t)s.k3) + 64 +
                                                  sizeof(int) * (8 + (size_t)s.k3));
         /* FP64 accumulation blocks (used by the tensor-core path, B = I) */
-        if (ctx->opt.accum64 && s.noB && ctx->opt.tensor_cores && s.k <= 64) {
+        const int split = ctx->opt.split_products && s.noY && s.dt == GPU_MV_FLOAT32;
+        if ((ctx->opt.accum64 || split) && s.noB && ctx->opt.tensor_cores && s.k <= 64) {
           for (int b = 0; b < 2; b++) {
             eb.X64[b] = gb_mv_create_like(s.X, GPU_MV_FLOAT64);
             eb.AX64[b] = gb_mv_create_like(s.X, GPU_MV_FLOAT64);
           }
           eb.Xout = Xu;
+          if (split) {
+            eb.RS = gb_mv_create_like(s.X, GPU_MV_FLOAT32);
+            /* Hx, Hr, Hp, Gr: the exact Grams the split pencil is built from */
+            eb.Hx = (double*)gb_device_alloc(ctx, sizeof(double) * 4 * (size_t)s.k3 * s.k3);
+          }
         }
         have_eb = 1;
         if (!eb.Xn || !eb.AXn || !eb.Pn || !eb.APn || !eb.G || (!s.noB && (!eb.BXn || !eb.BPn))) {
@@ -1300,9 +1455,11 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           gpu_MultiVectorDestroy(eb.X64[b]);
           gpu_MultiVectorDestroy(eb.AX64[b]);
         }
+        gpu_MultiVectorDestroy(eb.RS);
         if (eb.wrote_x64) x64_done = 1;
         gb_sync(ctx);
         gb_device_free(eb.G);
+        gb_device_free(eb.Hx);
       }
       if (!s.noY) {
         if (!s.noB && s.BY != s.Y) gpu_MultiVectorDestroy(s.BY);

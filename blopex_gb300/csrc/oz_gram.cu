@@ -1,12 +1,12 @@
 // oz_gram.cu -- FP64-accurate Gram products G = L' [L Q_0 Q_1 ...] on the
-// tensor cores by error-free splitting (oz_common.cuh): L an FP64 block of
-// h <= 64 columns (the Ritz block X of the mixed mode), Q_b blocks of up to 64
-// FP32 or FP64 columns (R, P).  It is serial_Multi_VectorInnerProd
-// (blopex_serial_double/multivector/multi_vector.c:354-406; the X rows of
-// gramB, lobpcg.c:1105-1160) with exact accumulation: the FP32 tensor-core
-// accumulators round toward zero, and summed over millions of rows that
-// bias is ~1e-5 relative, while these rows of the Gram matrix must be right
-// to ~1e-9 for the mixed mode to reach residuals of 1e-8.
+// tensor cores by error-free splitting (oz_common.cuh): L a block of h <= 64
+// FP32 or FP64 columns, Q_b blocks of up to 64 FP32 or FP64 columns.  It is
+// serial_Multi_VectorInnerProd (blopex_serial_double/multivector/
+// multi_vector.c:354-406; the Gram blocks of lobpcg.c:1092-1160) with exact
+// accumulation: FP32 tensor-core accumulators round toward zero, and summed
+// over millions of rows that bias is ~1e-5 relative; the mixed mode's pencil
+// breaks down (its R block stops being definite) with biased errors of 1e-6,
+// while unbiased errors of 1e-7 leave its convergence that of FP64.
 //
 // The contraction runs over n rows in chunks of 64.  Within a chunk every
 // column has its own power-of-two scale and is cut into S = 4 balanced
@@ -52,7 +52,7 @@
 
 struct ozg_params {
   blk_cols cols;       // tile b: L column c at cols.col[c]; Q_b column j at cols.col[64 + 64 b + j]
-  int h, nq;
+  int h, nq, ldt;                   // ldt: dtype of L (GPU_MV_*)
   int qw[OZG_MAXQ], qdt[OZG_MAXQ];  // widths and dtypes (GPU_MV_*) of the Q blocks
   long n;
   double* partial;  // [tile][cta][128][64]
@@ -65,7 +65,7 @@ static __device__ __forceinline__ int ozg_col_kind(const ozg_params& prm, int b,
   if (j < 64) {
     if (j >= prm.h) return 0;
     *ptr = prm.cols.col[j];
-    return 2;
+    return prm.ldt == GPU_MV_FLOAT64 ? 2 : 1;
   }
   const int q = j - 64;
   if (b >= prm.nq || q >= prm.qw[b]) return 0;
@@ -291,20 +291,23 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(buf * 256 + 32 * ihalf);
 #pragma unroll
       for (int g = 0; g < 4; g++) {
+        // the four level accumulators of these 8 columns, one wait for all
+        uint32_t r[OZG_S][8];
+#pragma unroll
+        for (int L = 0; L < OZG_S; L++)
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=r"(r[L][0]), "=r"(r[L][1]), "=r"(r[L][2]), "=r"(r[L][3]), "=r"(r[L][4]),
+                "=r"(r[L][5]), "=r"(r[L][6]), "=r"(r[L][7])
+              : "r"(tl + (uint32_t)(L * 64 + 8 * g)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         // Horner over the levels, highest first: v = sum_L S_L 2^(-7 L)
         float v[8];
 #pragma unroll
-        for (int L = OZG_S - 1; L >= 0; L--) {
-          uint32_t r[8];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                "=r"(r[7])
-              : "r"(tl + (uint32_t)(L * 64 + 8 * g)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int x = 0; x < 8; x++) {
+          v[x] = __uint_as_float(r[OZG_S - 1][x]);
 #pragma unroll
-          for (int x = 0; x < 8; x++)
-            v[x] = (L == OZG_S - 1) ? __uint_as_float(r[x]) : fmaf(v[x], 0.0078125f, __uint_as_float(r[x]));
+          for (int L = OZG_S - 2; L >= 0; L--) v[x] = fmaf(v[x], 0.0078125f, __uint_as_float(r[L][x]));
         }
 #pragma unroll
         for (int x = 0; x < 8; x++) {
@@ -368,8 +371,8 @@ __global__ void oz_gram_reduce_kernel(const double* __restrict__ partial, int gx
   G[i + (size_t)col * ldg] = s;
 }
 
-extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int nq, const blk_cols* Q,
-                          const int* qw, const int* qdt, double* G, int ldg)
+extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int ldt, int nq,
+                          const blk_cols* Q, const int* qw, const int* qdt, double* G, int ldg)
 {
   if (h < 1 || h > 64 || nq < 0 || nq > OZG_MAXQ || n <= 0)
     return gb_fail(ctx, "oz_gram: shape (h %d, %d blocks) not supported", h, nq);
@@ -377,6 +380,7 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
   memset(&prm, 0, sizeof(prm));
   prm.h = h;
   prm.nq = nq;
+  prm.ldt = ldt;
   prm.n = n;
   for (int c = 0; c < h; c++) {
     prm.cols.col[c] = L->col[c];
@@ -419,7 +423,7 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
   if (rc) return rc;
   oz_gram_reduce_kernel<<<(h * wtot + 255) / 256, 256, 0, (cudaStream_t)ctx->stream>>>(
       prm.partial, (int)gx, h, nq, qoff, wtot, G, ldg, prm.err);
-  double bytes = 8.0 * n * h;
+  double bytes = (ldt == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * h;
   for (int q = 0; q < nq; q++) bytes += (qdt[q] == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * qw[q];
   gb_prof_end(ctx, &pr, bytes, 2.0 * n * h * wtot);
   gb_count_launch(2);
@@ -431,7 +435,6 @@ extern "C" int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, do
 {
   gpu_Context* ctx = L->ctx;
   const int h = L->num_active;
-  if (L->dtype != GPU_MV_FLOAT64) return gb_fail(ctx, "SplitGram: L must be FP64");
   if (nq < 0 || nq > OZG_MAXQ) return gb_fail(ctx, "SplitGram: at most %d Q blocks", OZG_MAXQ);
   blk_cols cl;
   blk_cols* cq = (blk_cols*)malloc(sizeof(blk_cols) * (nq > 0 ? nq : 1));
@@ -455,7 +458,7 @@ extern "C" int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, do
   }
   double* d = (double*)gb_device_alloc(ctx, sizeof(double) * (size_t)h * wtot);
   int rc = d ? 0 : -1;
-  if (!rc) rc = gb_oz_gram(ctx, L->size, &cl, h, nq, cq, qw, qdt, d, h);
+  if (!rc) rc = gb_oz_gram(ctx, L->size, &cl, h, L->dtype, nq, cq, qw, qdt, d, h);
   double* hbuf = (double*)malloc(sizeof(double) * (size_t)h * wtot);
   if (!rc && !hbuf) rc = gb_fail(ctx, "SplitGram: out of host memory");
   if (!rc) rc = gb_memcpy_d2h(ctx, hbuf, d, sizeof(double) * (size_t)h * wtot);

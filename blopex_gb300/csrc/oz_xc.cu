@@ -36,6 +36,7 @@
 #define OZX_THREADS 512
 #define OZX_NPROD 256
 #define OZX_ASLICE 16384  // 128 rows x 128 bytes
+static_assert(OZX_S % 3 == 0, "the epilogue reads the levels three at a time");
 
 struct ozx_params {
   blk_cols x, y, z, y32;
@@ -268,22 +269,41 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
       const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16);
 #pragma unroll 1
       for (int g = 0; g < NW / 16; g++) {
+        // this row's 16 Z values: all loads in flight before the TMEM reads
+        unsigned long long zb[16];
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+          const int j = 16 * g + jj;
+          zb[jj] = 0;
+          if (row < prm.n && j < w) {
+            if (prm.z_kind == 1)
+              zb[jj] = __float_as_uint(((const float*)prm.z.col[j])[row]);
+            else if (prm.z_kind == 2)
+              zb[jj] = (unsigned long long)__double_as_longlong(((const double*)prm.z.col[j])[row]);
+          }
+        }
         long long T[16];
 #pragma unroll
         for (int jj = 0; jj < 16; jj++) T[jj] = 0;
+        // the S level accumulators of these 16 columns, two waits in all
 #pragma unroll
-        for (int L = 0; L < OZX_S; L++) {
-          uint32_t v[16];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-              "%13,%14,%15}, [%16];"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-                "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-              : "r"(tl + (uint32_t)(L * NW + 16 * g)));
+        for (int L0 = 0; L0 < OZX_S; L0 += 3) {
+          uint32_t v[3][16];
+#pragma unroll
+          for (int L = 0; L < 3; L++)
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+                "%13,%14,%15}, [%16];"
+                : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
+                  "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7]), "=r"(v[L][8]), "=r"(v[L][9]),
+                  "=r"(v[L][10]), "=r"(v[L][11]), "=r"(v[L][12]), "=r"(v[L][13]), "=r"(v[L][14]),
+                  "=r"(v[L][15])
+                : "r"(tl + (uint32_t)((L0 + L) * NW + 16 * g)));
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int jj = 0; jj < 16; jj++) T[jj] = T[jj] * 128 + oz_int_of(__uint_as_float(v[jj]));
+          for (int L = 0; L < 3; L++)
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) T[jj] = T[jj] * 128 + oz_int_of(__uint_as_float(v[L][jj]));
         }
         if (row < prm.n) {
 #pragma unroll
@@ -293,9 +313,9 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
             long long mz = 0;
             int ez = 0;
             if (prm.z_kind == 1)
-              oz_unpack32(((const float*)prm.z.col[j])[row], mz, ez);
+              oz_unpack32(__uint_as_float((uint32_t)zb[jj]), mz, ez);
             else if (prm.z_kind == 2)
-              oz_unpack64(((const double*)prm.z.col[j])[row], mz, ez);
+              oz_unpack64(__longlong_as_double((long long)zb[jj]), mz, ez);
             const int ec = colexp[j];
             double y;
             if (er == 0 || ec == 0) {

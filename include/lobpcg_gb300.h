@@ -60,6 +60,11 @@ typedef struct {
   int fp32_precond;         /* mixed: the inner-CG preconditioner (gpu_PCGPreconditionerCreate)
                                iterates on FP32 copies of FP64 blocks (the FP64 phase); the
                                preconditioner only shapes the search directions (0) */
+  int split_products;       /* mixed, tensor-core path (B = I, no constraints, k <= 64): carry X
+                               and A X in FP64 and form the products that decide the final
+                               residual FP64-accurately on the tensor cores (split-operand X C
+                               updates and X' [X R P] Gram rows), so the explicit phase itself
+                               iterates to the tolerance (1) */
 } lobpcg_gpu_options;
 
 typedef struct {
@@ -78,6 +83,13 @@ typedef struct {
   int rr_graded;            /* of those: pencils too graded for the tridiagonal solver */
   int explicit_undos;       /* mixed: FP32 steps undone after a residual jump */
   int explicit_p_drops;     /* mixed: FP32 steps taken without P (not definite / unresolved) */
+  int iterations_split;     /* mixed: explicit-phase iterations with FP64-carried X (split
+                               products) */
+  int handover_reason;      /* mixed: why the explicit phase handed over to the FP64 loop:
+                               0 it did not (converged or maxit), 1 residual below fp64_below,
+                               2 no progress, 3 block not definite, 4 Rayleigh-Ritz failed,
+                               5 residual jumps not repaired by undoing the step */
+  int device_errors;        /* tensor-core kernels that reported a timed-out wait */
 } lobpcg_gpu_stats;
 
 /* per-kernel-class timing, collected with CUDA events on the context's
@@ -215,12 +227,12 @@ int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_Multi
 
 /* G = L' [L Q_0 .. Q_{nq-1}] over the active columns, FP64-accurate on the
    tensor cores (error-free splitting of 64-row chunks into bf16 digits,
-   exact FP32 accumulation per chunk, unbiased sums across chunks): L FP64
-   with at most 64 active columns, each Q_b FP32 or FP64 with at most 64
+   exact FP32 accumulation per chunk, unbiased sums across chunks): L FP32 or
+   FP64 with at most 64 active columns, each Q_b FP32 or FP64 with at most 64
    (nq <= 4).  G_host (h x (h + sum of the Q widths), leading dimension ldg)
-   receives L'L and then each L'Q_b.  The X rows of the reference's gramB
-   (serial_Multi_VectorInnerProd, multi_vector.c:354-406, at lobpcg.c:
-   1105-1160) as the mixed mode forms them. */
+   receives L'L and then each L'Q_b.  The Gram blocks of the reference's
+   gramA / gramB (serial_Multi_VectorInnerProd, multi_vector.c:354-406, at
+   lobpcg.c:1092-1160) as the mixed mode forms them. */
 int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, double* G_host, int ldg);
 
 /* ---------------------------------------------------------------- */
@@ -311,7 +323,7 @@ int gpu_MassGradient(gpu_Operator* B, gpu_MultiVector* X, gpu_MultiVector* W,
  * calls no cudaMalloc, cudaFree or allocating library routine; the split-k
  * partial sums go to one fixed device array of GPU_GRAM_NOALLOC_MAX_DOUBLES
  * doubles (4 MiB) that every GPU which loads the library holds until exit.
- *   - h * w must not exceed that maximum and h, w must not exceed 384; larger
+ *   - h and w must not exceed 384 (so h * w stays below that maximum); larger
  *     sizes are rejected with return value -2 (nothing is launched).
  *   - The first call on a device looks the array's address up
  *     (cudaGetSymbolAddress) with that device current; make that first call
@@ -321,7 +333,9 @@ int gpu_MassGradient(gpu_Operator* B, gpu_MultiVector* X, gpu_MultiVector* W,
  *     by the caller.  The array keeps the last call's partial sums; every
  *     call overwrites all partials it reads, so nothing needs clearing.
  * Returns 0 on success, -1 for bad arguments, -2 for sizes beyond the
- * maximum, -3 for a CUDA error.
+ * maximum, -3 for a CUDA error (also when an error from earlier work on the
+ * calling thread is still pending; that error is left in place for its
+ * owner and nothing is launched).
  */
 #define GPU_GRAM_NOALLOC_MAX_DOUBLES (512 * 1024)
 int gpu_GramNoAlloc(int dtype, long n, const void* X, long ldx, int h, const void* Y, long ldy,

@@ -26,7 +26,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libblopex_ref.so")
-REF_SRC = os.environ.get("BLOPEX_REFERENCE_DIR", "/root/reference")
+# the reference checkout, when this machine has one (no default location)
+REF_SRC = os.environ.get("BLOPEX_REFERENCE_DIR", "")
 
 OP_NONE, OP_CSR, OP_DENSE, OP_DIAG, OP_STENCIL7, OP_STENCIL5, OP_STENCIL27 = range(7)
 
@@ -35,7 +36,7 @@ def build(ref: bool = True) -> None:
     """Compile the restatement (always) and the reference harness (when the
     reference checkout is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if ref and os.path.isdir(REF_SRC):
+    if ref and REF_SRC and os.path.isdir(REF_SRC):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
 
 

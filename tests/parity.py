@@ -7,8 +7,10 @@ flag, iteration count within 2, eigenvalues to 1e-10 relative.  Where the
 reference's own runs spread (rounding-chaotic cases: unconverged or
 degenerate clusters, non-invariant constraints, exactly singular blocks),
 the bar is that envelope: the exit flag of one of the runs, the iteration
-count within the runs' range widened by 2 + the spread, and eigenvalues
-within max(1e-10, 3 x the runs' spread) of the matching run.
+count within the range of the runs with that flag widened by 2 + their
+spread (at least a tenth of the count where the builds branch), and eigenvalues within max(1e-10, 3 x their spread) of the matching
+run (not checked only for a failure before the first iteration, where the
+reference leaves them unset).
 """
 import numpy as np
 
@@ -26,18 +28,18 @@ def check(g, flag, iterations, lam):
     rs = runs(g)
     same = [r for r in rs if r["flag"] == flag]
     assert same, f"exit flag {flag} not among the reference runs {[r['flag'] for r in rs]}"
-    if len({r["flag"] for r in rs}) > 1:
-        # the reference's own builds take different branches (e.g. an exactly
-        # singular block whose Cholesky pivot rounds to +eps or -eps): the
-        # iteration count after the branch carries no information; the
-        # eigenvalues of a converged run must still match
-        assert iterations <= max(r["iterations"] for r in rs) + g.get("maxit", 10 ** 9)
-        if flag != 0:
-            return
-        its = [iterations]
-    else:
-        its = [r["iterations"] for r in same]
+    # the runs that took the same exit as the GPU bound its iteration count;
+    # when the reference's own builds branch (e.g. an exactly singular block
+    # whose Cholesky pivot rounds to +eps in one build and -eps in another)
+    # only the branch the GPU took counts, and a converged GPU run is still
+    # held to that branch's eigenvalues below
+    its = [r["iterations"] for r in same]
     spread = max(its) - min(its)
+    if len({r["flag"] for r in rs}) > 1:
+        # after such a branch the trajectory is driven by rounding noise (an
+        # exactly rank-deficient block regains rank from it): the count may
+        # drift by a tenth beyond the branch's own runs
+        spread = max(spread, (max(its) + 9) // 10)
     lo, hi = min(its) - 2 - spread, max(its) + 2 + spread
     assert lo <= iterations <= hi, f"iterations {iterations} outside [{lo}, {hi}] ({its})"
     if iterations == 0 and flag != 0:

@@ -98,9 +98,9 @@ def test_split_update_exact_on_integers(ctx):
     assert np.array_equal(Y, X @ C + Z)
 
 
-def _gram(ctx, L, Qs):
+def _gram(ctx, L, Qs, ldt=S.FLOAT64):
     h = L.shape[1]
-    ml = S.MultiVector.from_host(ctx, L, S.FLOAT64)
+    ml = S.MultiVector.from_host(ctx, L, ldt)
     mqs = [S.MultiVector.from_host(ctx, q, dt) for q, dt in Qs]
     import ctypes
     arr = (ctypes.c_void_p * max(1, len(mqs)))(*[m.handle for m in mqs])
@@ -163,3 +163,18 @@ def test_split_gram_exact_on_integers(ctx):
     Q = rng.integers(-50, 51, size=(n, 40)).astype(np.float32).astype(np.float64)
     G = _gram(ctx, L, [(Q, S.FLOAT32)])
     assert np.array_equal(G, L.T @ np.hstack([L, Q]))
+
+
+def test_split_gram_fp32_left_block(ctx):
+    """L FP32 (the mixed mode's R and P blocks, nearly dependent columns):
+    R'[R AR] to the same bound."""
+    rng = np.random.default_rng(21)
+    n = 200003
+    base = rng.standard_normal((n, 4))
+    L = (base @ rng.standard_normal((4, 40)) + 1e-4 * rng.standard_normal((n, 40)))
+    L = L.astype(np.float32).astype(np.float64)
+    Q = rng.standard_normal((n, 64)).astype(np.float32).astype(np.float64)
+    G = _gram(ctx, L, [(Q, S.FLOAT32)], ldt=S.FLOAT32)
+    R = np.hstack([L, Q])
+    err = np.abs(G - L.T @ R)
+    assert np.all(err <= _bound_gram(L, R)), (err / _bound_gram(L, R)).max()
