@@ -57,6 +57,13 @@ CONFIGS = {
                label="matrix-free variable-coefficient 7-point stencil 256^3 (n=16777216), face "
                      "coefficients exp(N(0,1)) seed 2, k=64, X0 drand48 seed 2, tol 1e-8, "
                      "preconditioner 20 Jacobi-CG steps on A"),
+    # the same operator family at 128^3: a full solve takes seconds, so it can
+    # be repeated as the timed step; the 256^3 case runs once beside it
+    "c3m": dict(kind="stencil7", grid=(128, 128, 128), k=64, seed=2, tol=1e-8, maxit=1000,
+                jacobi=True, precond="pcg20", full="c3",
+                label="matrix-free variable-coefficient 7-point stencil 128^3 (n=2097152), face "
+                      "coefficients exp(N(0,1)) seed 2, k=64, X0 drand48 seed 2, tol 1e-8, "
+                      "preconditioner 20 Jacobi-CG steps on A"),
 }
 
 
@@ -208,9 +215,9 @@ def build_problem(cfg, grid=None):
     return n, op, x0, tdiag
 
 
-def cpu_baseline(cfg, iterations=None):
+def cpu_baseline(cfg, iterations=None, sample_grid=32):
     """The oracle (C restatement of the reference, scalar loops, one core) on
-    a bounded sample: a 32^3 grid with the same k and a Jacobi
+    a bounded sample: a 32^3 grid (24^3 for the reference arm) with the same k and a Jacobi
     preconditioner, 1 and 3 iterations; the per-iteration time is scaled by n
     (the work per iteration is linear in n at fixed k) to the full grid and
     multiplied by the iteration count of the FP64 GPU path on the workload
@@ -225,7 +232,7 @@ def cpu_baseline(cfg, iterations=None):
     O.build(ref=False)
     nx, ny, nz = cfg["grid"]
     n_full = nx * ny * nz
-    s = min(32, nx)
+    s = min(sample_grid, nx)
     n, op, x0, tdiag = build_problem(dict(cfg, jacobi=True), (s, s, s))
     csr = op[1] if op[0] == "csr" else P.stencil7_to_csr(*op[1])
     A = O.csr(*csr)
@@ -369,8 +376,8 @@ def run_reference(args, cfg):
     if rank != 0:
         return
     for _ in range(args.warmup):
-        cpu_baseline(cfg)
-    vals = [cpu_baseline(cfg) for _ in range(args.steps)]  # each a bounded sample
+        cpu_baseline(cfg, sample_grid=24)
+    vals = [cpu_baseline(cfg, sample_grid=24) for _ in range(args.steps)]  # each a bounded sample
     v = statistics.median(x["value"] for x in vals)
     cb = dict(vals[0])
     cb["value"] = v
@@ -437,7 +444,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c3m", choices=sorted(CONFIGS))
     ap.add_argument("--mode", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--maxit", type=int, default=0, help="override maxit (exploration only)")
     ap.add_argument("--precond", default="",
@@ -446,6 +453,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end repetition")
     ap.add_argument("--grid", type=int, default=0,
                     help="override the grid edge (small cases for profiling only)")
+    ap.add_argument("--no-full", action="store_true",
+                    help="skip the once-measured full-size comparison (config key 'full')")
     ap.add_argument("--no-other-arm", action="store_true",
                     help="skip the other precision's arm (FP64 beside mixed or the reverse)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -538,7 +547,7 @@ def main():
         pinned_out = torch.empty(n * k, dtype=torch.float64).pin_memory()
         ctx.set_options(precision=S.FP64 if args.mode == "fp64" else S.MIXED)
         e2e_times = []
-        for _ in range(max(1, args.steps)):
+        for _ in range(min(max(1, args.steps), 3)):  # median of up to 3 steps
             barrier()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -631,14 +640,68 @@ def main():
                                              "d2h_bytes_per_step": n * k * 8 + 2 * k * 8},
             "gpu_launches": int(launches),
             "clocks": clocks}
+    full = None
+    if cfg.get("full") and not args.no_full:
+        X0.close()
+        X.close()
+        ctx.lib.gpu_ContextTrim(ctx.handle)
+        full = run_full(dict(CONFIGS[cfg["full"]]), ctx, S, torch, stream, precond)
+        line["full_size"] = full
     if rank == 0 and not args.no_cpu:
         fp64_its = (other["iterations"] if (other and other_mode == "fp64")
                     else (res.iterations if args.mode == "fp64" else None))
         line["cpu_baseline"] = cpu_baseline(cfg, fp64_its)
+        if full and full.get("fp64"):
+            line["full_size"]["cpu_baseline"] = cpu_baseline(dict(CONFIGS[cfg["full"]]),
+                                                             full["fp64"]["iterations"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_full(cfg, ctx, S, torch, stream, precond):
+    """The full-size configuration measured once per arm: mixed precision and
+    the plain FP64 GPU path, each from the same X0 to the tolerance (after a
+    3-iteration warm-up of its kernels), with the eigenvalue error, the
+    largest subspace angle between the two blocks and X'X - I."""
+    n, op, x0, tdiag = build_problem(cfg)
+    k = cfg["k"]
+    A = S.Stencil7(ctx, *op[1]) if op[0] == "stencil7" else S.CSRMatrix(ctx, *op[1])
+    T = S.Diagonal(ctx, tdiag) if tdiag is not None else None
+    if precond.startswith("pcg"):
+        T = S.PCGPreconditioner(ctx, A, T, int(precond[3:]))
+    X0 = S.MultiVector(ctx, n, k)
+    if x0 is not None:
+        X0.upload(x0)
+    else:
+        X0.set_random(cfg["seed"])
+    out = {"workload": cfg["label"], "n": n, "k": k, "tol": cfg["tol"], "maxit": cfg["maxit"]}
+    blocks, results = {}, {}
+    for mode in ("mixed", "fp64"):
+        Xm = S.MultiVector(ctx, n, k)
+        ctx.set_options(precision=S.FP64 if mode == "fp64" else S.MIXED)
+        Xm.copy_from(X0)
+        S.lobpcg_solve_double(Xm, A, T=T, atol=cfg["tol"], rtol=1e-50, maxit=3, history=False)
+        Xm.copy_from(X0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = S.lobpcg_solve_double(Xm, A, T=T, atol=cfg["tol"], rtol=1e-50, maxit=cfg["maxit"],
+                                  history=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[mode] = dict(arm_summary(r, e0.elapsed_time(e1) / 1e3),
+                         orthonormality_fro=orthonormality(ctx, S, Xm))
+        blocks[mode], results[mode] = Xm, r
+    out["comparison"] = compare_arms(ctx, S, blocks["mixed"], blocks["fp64"], results["mixed"],
+                                     results["fp64"])
+    out["mixed_speedup_over_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    for b in blocks.values():
+        b.close()
+    X0.close()
+    return out
 
 
 def arm_summary(r, seconds):
@@ -651,6 +714,7 @@ def arm_summary(r, seconds):
             "iterations_fp64_loop": st["iterations_fp64"],
             "iterations_compensated": st["iterations_compensated"],
             "explicit_undos": st["explicit_undos"], "explicit_p_drops": st["explicit_p_drops"],
+            "handover_reason": st["handover_reason"], "device_errors": st["device_errors"],
             "seconds_explicit_phase": st["seconds_fp32"], "seconds_fp64_loop": st["seconds_fp64"]}
 
 

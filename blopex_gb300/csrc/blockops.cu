@@ -617,14 +617,16 @@ extern "C" int gb_accumulate64(gpu_Context* ctx, long n, const blk_cols* X64, co
 //   Hx = X'[X R P]          (k x m, ld k)
 //   Hr = R'[R P AR AP]      (nR x (2 nR + 2 nP), ld nR)
 //   Hp = P'[P AP]           (nP x 2 nP, ld nP)
-//   Gr = RS'[RS X R P]      (k x (k + m), ld k), RS = lambda X - A X
+//   Gt(c, i) = S_c' RS_i    (ld ld; column i < k of the tensor-core product
+//                            [X R P]'[RS AR AP]), RS = lambda X - A X
 // with lambda the Rayleigh quotients of X.  The X rows of G are formed in
 // residual form, G(i, c) = X_i' A S_c = lambda_i X_i' S_c - RS_i' S_c, so that
-// A X (whose norm is the spectrum's scale) never enters a product; the other
-// blocks are R'AR, R'AP, P'AP.  Symmetric blocks are averaged with their
-// transposes.
+// A X (whose norm is the spectrum's scale) never enters a product and the
+// rounding of RS'S scales with the residual (TF32 products suffice there);
+// the other blocks are R'AR, R'AP, P'AP.  Symmetric blocks are averaged with
+// their transposes.
 __global__ void split_pencil_kernel(const double* __restrict__ Hx, const double* __restrict__ Hr,
-                                    const double* __restrict__ Hp, const double* __restrict__ Gr,
+                                    const double* __restrict__ Hp, const double* __restrict__ Gt,
                                     double* G, double* H, int ld, const double* __restrict__ lam,
                                     int k, int nR, int nP)
 {
@@ -637,11 +639,11 @@ __global__ void split_pencil_kernel(const double* __restrict__ Hx, const double*
     if (a < k && b < k) {
       const double h1 = Hx[a + (size_t)b * k], h2 = Hx[b + (size_t)a * k];
       h = 0.5 * (h1 + h2);
-      g = 0.5 * ((lam[a] * h1 - Gr[a + (size_t)(k + b) * k]) + (lam[b] * h2 - Gr[b + (size_t)(k + a) * k]));
+      g = 0.5 * ((lam[a] * h1 - Gt[b + (size_t)a * ld]) + (lam[b] * h2 - Gt[a + (size_t)b * ld]));
     } else {
       const int i = a < k ? a : b, c = a < k ? b : a;
       h = Hx[i + (size_t)c * k];
-      g = lam[i] * h - Gr[i + (size_t)(k + c) * k];
+      g = lam[i] * h - Gt[c + (size_t)i * ld];
     }
   } else {
     const int ra = a - k, rb = b - k;  // offsets in [R P]
@@ -664,11 +666,11 @@ __global__ void split_pencil_kernel(const double* __restrict__ Hx, const double*
 }
 
 extern "C" int gb_split_pencil(gpu_Context* ctx, const double* Hx, const double* Hr, const double* Hp,
-                               const double* Gr, double* G, double* H, int ld, const double* lam, int k,
+                               const double* Gt, double* G, double* H, int ld, const double* lam, int k,
                                int nR, int nP)
 {
   const int m = k + nR + nP;
-  split_pencil_kernel<<<(m * m + 255) / 256, 256, 0, S(ctx)>>>(Hx, Hr, Hp, Gr, G, H, ld, lam, k, nR, nP);
+  split_pencil_kernel<<<(m * m + 255) / 256, 256, 0, S(ctx)>>>(Hx, Hr, Hp, Gt, G, H, ld, lam, k, nR, nP);
   gb_count_launch(1);
   return CUDA_LAUNCH_CHECK(ctx, "split pencil");
 }

@@ -818,10 +818,16 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       double lg = 0.0;
       for (int i = 0; i < k; i++) lg += log(s->h_norm[i] + DBL_MIN);
       lg /= k;
+      /* split mode has no FP32 floor to detect: its residuals plateau as
+         long as the FP64 loop's do (minutes on a 256^3 problem), so only a
+         long stretch without progress -- shorter near the tolerance, where a
+         precision floor would show -- hands over */
+      const int limit = !split ? ctl->stall_limit
+                        : (mx < 100.0 * s->tol.absolute ? 30 : 5 * ctl->stall_limit);
       if (lg < best - 1e-3) {
         best = lg;
         stall = 0;
-      } else if (++stall >= ctl->stall_limit) {
+      } else if (++stall >= limit) {
         if (tc_ok && !comp) {
           comp = 1; /* TF32 products stalled: compensate before FP64 */
           stall = 0;
@@ -890,10 +896,11 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       cols_idx(AP, act, nP, &right, off);
       if (split) {
         /* the whole pencil from exact Grams (split-operand tensor-core
-           products): X'[X R P], R'[R P AR AP], P'[P AP], RS'[RS X R P] */
+           products): X'[X R P], R'[R P AR AP], P'[P AP]; the X rows of G in
+           residual form */
         const int F32 = GPU_MV_FLOAT32, F64 = GPU_MV_FLOAT64;
         const size_t sq = (size_t)k3 * k3;
-        double *Hx = eb->Hx, *Hr = Hx + sq, *Hp = Hr + sq, *Gr = Hp + sq;
+        double *Hx = eb->Hx, *Hr = Hx + sq, *Hp = Hr + sq;
         blk_cols cq[3];
         int qw[3], qdt[3], nq;
         blk_cols cl;
@@ -913,13 +920,23 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
           cols_idx(AP, act, nP, &cq[0], 0), qw[0] = nP, qdt[0] = F32;
           if (gb_oz_gram(s->ctx, s->n, &cl, nP, F32, 1, cq, qw, qdt, Hp, nP)) return -2;
         }
-        cols_idx(eb->RS, NULL, k, &cl, 0);
-        nq = 0;
-        cols_idx(X64, NULL, k, &cq[nq], 0), qw[nq] = k, qdt[nq++] = F64;
-        cols_idx(R, NULL, nR, &cq[nq], 0), qw[nq] = nR, qdt[nq++] = F32;
-        if (nP) cols_idx(P, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
-        if (gb_oz_gram(s->ctx, s->n, &cl, k, F32, nq, cq, qw, qdt, Gr, k)) return -2;
-        if (gb_split_pencil(s->ctx, Hx, Hr, Hp, Gr, eb->G, eb->H, k3, s->lam, k, nR, nP)) return -2;
+        {
+          /* S' RS: small (it scales with the residual), so the TF32
+             tensor-core product carries enough accuracy; its H output is not
+             used (the exact one above is) */
+          blk_cols cx, cr, cp, cax, car, cap;
+          cols_idx(X, NULL, k, &cx, 0);
+          cols_idx(R, NULL, nR, &cr, 0);
+          cols_idx(P, act, nP, &cp, 0);
+          cols_idx(eb->RS, NULL, k, &cax, 0);
+          cols_idx(AR, NULL, nR, &car, 0);
+          cols_idx(AP, act, nP, &cap, 0);
+          if (gb_tc_gram(s->ctx, s->n, &cx, k, &cr, nR, &cp, nP, &cax, &car, &cap, 1, eb->tmp,
+                         eb->H2, k3))
+            return -2;
+        }
+        if (gb_split_pencil(s->ctx, Hx, Hr, Hp, eb->tmp, eb->G, eb->H, k3, s->lam, k, nR, nP))
+          return -2;
         s->ctx->stats.iterations_split++;
       } else if (tc_ok) {
         blk_cols cx, cr, cp, cax, car, cap;
@@ -1378,8 +1395,8 @@ static int solve_gpu(gpu_MultiVector* Xu, void* Adata, op_fn A, void* Bdata, op_
           eb.Xout = Xu;
           if (split) {
             eb.RS = gb_mv_create_like(s.X, GPU_MV_FLOAT32);
-            /* Hx, Hr, Hp, Gr: the exact Grams the split pencil is built from */
-            eb.Hx = (double*)gb_device_alloc(ctx, sizeof(double) * 4 * (size_t)s.k3 * s.k3);
+            /* Hx, Hr, Hp: the exact Grams the split pencil is built from */
+            eb.Hx = (double*)gb_device_alloc(ctx, sizeof(double) * 3 * (size_t)s.k3 * s.k3);
           }
         }
         have_eb = 1;

@@ -9,16 +9,16 @@
 // left factor, a column of the right one, a column over a 64-row chunk) is
 // written in fixed point with F = 7 s fractional bits,
 //     v ~= 2^E * sum_t d_t 2^(-7 (t + 1)),   t = 0 .. s-1,
-// with balanced integer digits d_0 in [-129, 129] and d_t in [-64, 63]
-// (t >= 1), each held exactly by a bf16.  A digit product has at most 14
+// with integer digits of at most 128 in magnitude (rounded, so mostly within
+// +-64), each held exactly by a bf16.  A digit product has at most 14
 // bits, so the sums of digit products over a short contraction stay below
 // 2^22 and the tensor cores' FP32 accumulation is exact: the products of
 // level L = t + u are summed in one TMEM accumulator, and only the levels
 // L < s are formed (the rest lie below 2^(-7 s) of the scale).
 //
-// Everything between the FP64 values and the digits, and back, is integer
-// arithmetic on the bit patterns: this GPU's FP64 pipe runs at 1/64 of its
-// FP32 rate, so no FP64 instruction is spent per element.
+// Everything between the FP64 values and the digits, and back, is integer or
+// FP32 arithmetic on the bit patterns: this GPU's FP64 pipe runs at 1/64 of
+// its FP32 rate, so no FP64 instruction is spent per element.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -203,4 +203,64 @@ static __device__ __forceinline__ float oz_to_float(double v)
   }
   if (e >= 255) return __uint_as_float((sign << 31) | 0x7F800000u);
   return __uint_as_float((sign << 31) | ((uint32_t)e << 23) | (m24 & 0x7FFFFFu));
+}
+
+// ------------------------------------------- four digits with FP32 arithmetic
+// The same balanced 7-bit digits (S = 4, 28 fraction bits), cut with FP32
+// round-to-nearest arithmetic instead of integer shifts: rint(x) is
+// (x + 1.5 * 2^23) - 1.5 * 2^23 for |x| < 2^22, and every remainder is
+// formed exactly by an FMA.  The digits come out as floats holding small
+// integers (|d| <= 128) whose bf16 patterns are their top 16 bits.
+//   u = v 2^(28 - (E - 1022)),  |u| < 2^28
+//   h = rint(u / 2^14), l = u - 2^14 h
+//   d0 = rint(h / 2^7), d1 = h - 2^7 d0, d2 = rint(l / 2^7), d3 = rint(l - 2^7 d2)
+// so u ~= 2^21 d0 + 2^14 d1 + 2^7 d2 + d3 to within 1/2.
+
+#define OZ_RINT_MAGIC 12582912.0f  // 1.5 * 2^23
+
+static __device__ __forceinline__ void oz_digits4_hl(float h, float l, float (&d)[4])
+{
+  d[0] = fmaf(h, 0.0078125f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+  d[1] = fmaf(d[0], -128.0f, h);
+  d[2] = fmaf(l, 0.0078125f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+  d[3] = (fmaf(d[2], -128.0f, l) + OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+}
+
+// FP32 value; scale = 2^(28 - (E - 1022)) as a float (E in [923, 1176])
+static __device__ __forceinline__ void oz_digits4_f32(float v, float scale, float (&d)[4])
+{
+  const float u = v * scale;
+  const float h = fmaf(u, 0.00006103515625f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;  // 2^-14
+  const float l = fmaf(h, -16384.0f, u);
+  oz_digits4_hl(h, l, d);
+}
+
+// the scale of oz_digits4_f32 for a group exponent E, 0 when E is outside the
+// range the float can hold (the caller then takes the integer path)
+static __device__ __forceinline__ float oz_scale4(int E)
+{
+  const int f = 28 + 1022 - E + 127;
+  return (f >= 1 && f <= 254) ? __uint_as_float((uint32_t)f << 23) : 0.0f;
+}
+
+// a 28-bit fixed point magnitude U (<= 2^28) with sign bit sg (bit 31): its
+// two 14-bit halves as exact floats, then the digits (here l is in
+// [0, 2^14), so d2 reaches 128; the digit products stay below 2^14)
+static __device__ __forceinline__ void oz_digits4_u(uint32_t U, uint32_t sg, float (&d)[4])
+{
+  const float h = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (U >> 14)) - 8388608.0f) ^ sg);
+  const float l = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (U & 0x3FFFu)) - 8388608.0f) ^ sg);
+  oz_digits4_hl(h, l, d);
+}
+
+// FP64 value: the 28-bit fixed point integer from its bits, then as above
+static __device__ __forceinline__ void oz_digits4_f64(double v, int E, float (&d)[4])
+{
+  oz_digits4_u((uint32_t)oz_fixed64<28>(v, E), (uint32_t)((uint64_t)__double_as_longlong(v) >> 63) << 31, d);
+}
+
+// two digits (floats holding integers) as one word of two bf16 patterns
+static __device__ __forceinline__ uint32_t oz_pack_bf16(float lo, float hi)
+{
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }

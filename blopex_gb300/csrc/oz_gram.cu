@@ -9,9 +9,9 @@
 // while unbiased errors of 1e-7 leave its convergence that of FP64.
 //
 // The contraction runs over n rows in chunks of 64.  Within a chunk every
-// column has its own power-of-two scale and is cut into S = 4 balanced
-// 7-bit digits (28 fraction bits); level L = t + u of the digit products is
-// summed exactly in FP32 in TMEM (|sum| < 2^21).  After each chunk the four
+// column has its own power-of-two scale and is cut into S = 4 7-bit digits
+// (28 fraction bits; FP32 arithmetic, oz_digits4_*); level L = t + u of the
+// digit products is summed exactly in FP32 in TMEM (|sum| < 2^22).  After each chunk the four
 // levels are combined (FP32, round to nearest), scaled, and added into
 // double-float (hi + lo FP32) accumulators, so the chunk sums add without
 // bias; each CTA writes its sums in FP64 and a second kernel adds the CTAs
@@ -83,6 +83,10 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag, never_flag;
   __shared__ int part[1024];       // per (column, 8-row group) largest exponent
+  // this tile's column pointers and kinds (0 absent, 1 FP32, 2 FP64) in shared
+  // memory: a runtime index into the kernel-parameter table is slow
+  __shared__ const void* s_col[128];
+  __shared__ int s_kind[128];
   __shared__ int cexp[4][128];     // chunk scales, by chunk modulo 4
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -90,6 +94,11 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   const long nchunks = (prm.n + OZG_ROWS - 1) / OZG_ROWS;
   const long my_chunks = (long)blockIdx.x < nchunks ? (nchunks - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
+  if (tid < 128) {
+    const void* ptr = nullptr;
+    s_kind[tid] = ozg_col_kind(prm, b, tid, &ptr);
+    s_col[tid] = ptr;
+  }
   if (tid == 0) {
     abort_flag = 0;
     never_flag = 0;
@@ -119,6 +128,11 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   if (warp == 1) {
     // ------------------------------------------------------- bulk copies
     long issued[2] = {0, 0};  // chunks issued per slot
+    int ncol8 = 0, ncol4 = 0;  // FP64 and FP32 columns of this tile
+    for (int j = 0; j < 128; j++) {
+      ncol8 += s_kind[j] == 2;
+      ncol4 += s_kind[j] == 1;
+    }
     for (long c = 0; c < my_chunks; c++) {
       const int slot = (int)(c & 1);
       int stop = 0;
@@ -134,18 +148,13 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       const long rows = min((long)OZG_ROWS, prm.n - r0);
       // every column's copy covers whole 16-byte pieces
       const uint32_t b8 = (uint32_t)(((rows + 1) & ~1L) * 8), b4 = (uint32_t)(((rows + 3) & ~3L) * 4);
-      uint32_t total = 0;
-      for (int j = 0; j < 128; j++) {
-        const void* ptr;
-        const int kind = ozg_col_kind(prm, b, j, &ptr);
-        total += kind == 2 ? b8 : (kind == 1 ? b4 : 0u);
-      }
+      const uint32_t total = (uint32_t)ncol8 * b8 + (uint32_t)ncol4 * b4;
       if (lane == 0) mbar_expect_tx(&raw_full[slot], total);
       __syncwarp();
       unsigned char* raw = raws + slot * OZG_RAW;
       for (int j = lane; j < 128; j += 32) {
-        const void* ptr;
-        const int kind = ozg_col_kind(prm, b, j, &ptr);
+        const void* ptr = s_col[j];
+        const int kind = s_kind[j];
         if (kind == 2)
           bulk_g2s(raw + j * OZG_COLSTRIDE, (const double*)ptr + r0, b8, &raw_full[slot]);
         else if (kind == 1)
@@ -173,8 +182,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       // pass 1: largest exponent of each (column, 8-row group)
       for (int u = p; u < 1024; u += OZG_NPROD) {
         const int j = u >> 3, q = u & 7;
-        const void* ptr;
-        const int kind = abort_flag ? 0 : ozg_col_kind(prm, b, j, &ptr);
+        const int kind = abort_flag ? 0 : s_kind[j];
         int e = 0;
         for (int k = 0; k < 8 && kind; k++) {
           const int rr = 8 * q + k;
@@ -198,34 +206,38 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
           int E = 0;
 #pragma unroll
           for (int g = 0; g < 8; g++) E = max(E, part[8 * j + g]);
-          const void* ptr;
-          const int kind = ozg_col_kind(prm, b, j, &ptr);
+          const int kind = s_kind[j];
+          // the eight rows' digits with FP32 arithmetic (integer fixed point
+          // first for FP64 values, or for FP32 groups whose scale leaves the
+          // float range)
+          float dg[8][OZG_S];
+          const float sc = oz_scale4(E);
+          const double* c64 = (const double*)(raw + j * OZG_COLSTRIDE) + 8 * q;
+          const float* c32 = (const float*)(raw + j * OZG_COLSTRIDE) + 8 * q;
+          const int nr = min(8, rows - 8 * q);
+          if (kind == 1 && sc != 0.0f) {
+#pragma unroll
+            for (int x = 0; x < 8; x++) oz_digits4_f32(x < nr ? c32[x] : 0.0f, sc, dg[x]);
+          } else if (kind == 2) {
+#pragma unroll
+            for (int x = 0; x < 8; x++) oz_digits4_f64(x < nr ? c64[x] : 0.0, E, dg[x]);
+          } else if (kind == 1) {
+#pragma unroll
+            for (int x = 0; x < 8; x++) {
+              const float v = x < nr ? c32[x] : 0.0f;
+              oz_digits4_u((uint32_t)oz_fixed32<OZG_F>(v, E), __float_as_uint(v) & 0x80000000u, dg[x]);
+            }
+          } else {
+#pragma unroll
+            for (int x = 0; x < 8; x++)
+#pragma unroll
+              for (int t = 0; t < OZG_S; t++) dg[x][t] = 0.0f;
+          }
           uint32_t pk[OZG_S][4];
 #pragma unroll
-          for (int k = 0; k < 8; k += 2) {
-            uint32_t d0[OZG_S], d1[OZG_S];
+          for (int t = 0; t < OZG_S; t++)
 #pragma unroll
-            for (int x = 0; x < 2; x++) {
-              const int rr = 8 * q + k + x;
-              uint64_t U = 0;
-              uint32_t neg = 0;
-              if (kind == 2 && rr < rows) {
-                const double v = ((const double*)(raw + j * OZG_COLSTRIDE))[rr];
-                U = oz_fixed64<OZG_F>(v, E);
-                neg = (uint32_t)((uint64_t)__double_as_longlong(v) >> 63);
-              } else if (kind == 1 && rr < rows) {
-                const float v = ((const float*)(raw + j * OZG_COLSTRIDE))[rr];
-                U = oz_fixed32<OZG_F>(v, E);
-                neg = __float_as_uint(v) >> 31;
-              }
-              if (x == 0)
-                oz_digits<OZG_S>(U, neg, d0);
-              else
-                oz_digits<OZG_S>(U, neg, d1);
-            }
-#pragma unroll
-            for (int t = 0; t < OZG_S; t++) pk[t][k >> 1] = d0[t] | (d1[t] << 16);
-          }
+            for (int k = 0; k < 4; k++) pk[t][k] = oz_pack_bf16(dg[2 * k][t], dg[2 * k + 1][t]);
           const uint32_t off = (uint32_t)j * 128u + ((uint32_t)(q ^ (j & 7)) << 4);
 #pragma unroll
           for (int t = 0; t < OZG_S; t++)
