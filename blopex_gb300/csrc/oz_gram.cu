@@ -73,6 +73,23 @@ static __device__ __forceinline__ int ozg_col_kind(const ozg_params& prm, int b,
   return prm.qdt[b] == GPU_MV_FLOAT64 ? 2 : 1;
 }
 
+// eight consecutive values of a staged column (16-byte aligned) with 16-byte
+// shared-memory loads
+static __device__ __forceinline__ void ozg_load8(const unsigned char* src, double (&v)[8])
+{
+#pragma unroll
+  for (int x = 0; x < 4; x++) {
+    const double2 d = ((const double2*)src)[x];
+    v[2 * x] = d.x;
+    v[2 * x + 1] = d.y;
+  }
+}
+static __device__ __forceinline__ void ozg_load8(const unsigned char* src, float (&v)[8])
+{
+  const float4 a = ((const float4*)src)[0], b = ((const float4*)src)[1];
+  v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+}
+
 __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_constant__ ozg_params prm)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -82,7 +99,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag, never_flag;
-  __shared__ int part[1024];       // per (column, 8-row group) largest exponent
+  __shared__ __align__(16) int part[1024];  // per (column, 8-row group) largest exponent
   // this tile's column pointers and kinds (0 absent, 1 FP32, 2 FP64) in shared
   // memory: a runtime index into the kernel-parameter table is slow
   __shared__ const void* s_col[128];
@@ -179,16 +196,25 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       const long r0 = (blockIdx.x + c * gridDim.x) * OZG_ROWS;
       const int rows = (int)min((long)OZG_ROWS, prm.n - r0);
       const unsigned char* raw = raws + slot * OZG_RAW;
-      // pass 1: largest exponent of each (column, 8-row group)
+      // pass 1: largest exponent of each (column, 8-row group), the group's
+      // eight values read with 16-byte loads
       for (int u = p; u < 1024; u += OZG_NPROD) {
         const int j = u >> 3, q = u & 7;
         const int kind = abort_flag ? 0 : s_kind[j];
+        const int nr = min(8, rows - 8 * q);
         int e = 0;
-        for (int k = 0; k < 8 && kind; k++) {
-          const int rr = 8 * q + k;
-          if (rr >= rows) break;
-          e = max(e, kind == 2 ? oz_bexp64(((const double*)(raw + j * OZG_COLSTRIDE))[rr])
-                               : oz_bexp32(((const float*)(raw + j * OZG_COLSTRIDE))[rr]));
+        if (kind == 2) {
+          double v[8];
+          ozg_load8(raw + j * OZG_COLSTRIDE + 64 * q, v);
+#pragma unroll
+          for (int x = 0; x < 8; x++)
+            if (x < nr) e = max(e, oz_bexp64(v[x]));
+        } else if (kind == 1) {
+          float v[8];
+          ozg_load8(raw + j * OZG_COLSTRIDE + 32 * q, v);
+#pragma unroll
+          for (int x = 0; x < 8; x++)
+            if (x < nr) e = max(e, oz_bexp32(v[x]));
         }
         part[u] = e;
       }
@@ -203,30 +229,33 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
         // pass 2: the digits of (column j, rows 8q .. 8q + 7)
         for (int u = p; u < 1024; u += OZG_NPROD) {
           const int j = u >> 3, q = u & 7;
-          int E = 0;
-#pragma unroll
-          for (int g = 0; g < 8; g++) E = max(E, part[8 * j + g]);
+          const int4 pa = *(const int4*)&part[8 * j], pb = *(const int4*)&part[8 * j + 4];
+          const int E = max(max(max(pa.x, pa.y), max(pa.z, pa.w)), max(max(pb.x, pb.y), max(pb.z, pb.w)));
           const int kind = s_kind[j];
           // the eight rows' digits with FP32 arithmetic (integer fixed point
           // first for FP64 values, or for FP32 groups whose scale leaves the
           // float range)
           float dg[8][OZG_S];
           const float sc = oz_scale4(E);
-          const double* c64 = (const double*)(raw + j * OZG_COLSTRIDE) + 8 * q;
-          const float* c32 = (const float*)(raw + j * OZG_COLSTRIDE) + 8 * q;
           const int nr = min(8, rows - 8 * q);
-          if (kind == 1 && sc != 0.0f) {
+          if (kind == 1) {
+            float v[8];
+            ozg_load8(raw + j * OZG_COLSTRIDE + 32 * q, v);
 #pragma unroll
-            for (int x = 0; x < 8; x++) oz_digits4_f32(x < nr ? c32[x] : 0.0f, sc, dg[x]);
-          } else if (kind == 2) {
+            for (int x = 0; x < 8; x++) v[x] = x < nr ? v[x] : 0.0f;
+            if (sc != 0.0f) {
 #pragma unroll
-            for (int x = 0; x < 8; x++) oz_digits4_f64(x < nr ? c64[x] : 0.0, E, dg[x]);
-          } else if (kind == 1) {
+              for (int x = 0; x < 8; x++) oz_digits4_f32(v[x], sc, dg[x]);
+            } else {
 #pragma unroll
-            for (int x = 0; x < 8; x++) {
-              const float v = x < nr ? c32[x] : 0.0f;
-              oz_digits4_u((uint32_t)oz_fixed32<OZG_F>(v, E), __float_as_uint(v) & 0x80000000u, dg[x]);
+              for (int x = 0; x < 8; x++)
+                oz_digits4_u((uint32_t)oz_fixed32<OZG_F>(v[x], E), __float_as_uint(v[x]) & 0x80000000u, dg[x]);
             }
+          } else if (kind == 2) {
+            double v[8];
+            ozg_load8(raw + j * OZG_COLSTRIDE + 64 * q, v);
+#pragma unroll
+            for (int x = 0; x < 8; x++) oz_digits4_f64(x < nr ? v[x] : 0.0, E, dg[x]);
           } else {
 #pragma unroll
             for (int x = 0; x < 8; x++)
