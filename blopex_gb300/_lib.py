@@ -30,7 +30,8 @@ class Options(ctypes.Structure):
                 ("sygv_fail_at", c_int), ("explicit_pivot_below", c_double),
                 ("fp32_accurate_op", c_int), ("recompute_ap", c_int), ("explicit_fp64", c_int),
                 ("accum64", c_int),
-                ("rr_method", c_int), ("fp32_precond", c_int), ("split_products", c_int)]
+                ("rr_method", c_int), ("fp32_precond", c_int), ("split_products", c_int),
+                ("wait_polls", c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -129,6 +130,7 @@ SIGNATURES = {
     "gpu_ContextSetOptions": (c_int, [c_void_p, ctypes.POINTER(Options)]),
     "gpu_ContextGetStats": (None, [c_void_p, ctypes.POINTER(Stats)]),
     "gpu_ContextLastError": (ctypes.c_char_p, [c_void_p]),
+    "gpu_ContextDeviceError": (c_int, [c_void_p, c_void_p]),
     "gpu_ContextSetProfiling": (c_int, [c_void_p, c_int]),
     "gpu_ContextKernelTimes": (c_int, [c_void_p, ctypes.POINTER(KernelTime), c_int]),
     "gpu_ContextResetKernelTimes": (None, [c_void_p]),

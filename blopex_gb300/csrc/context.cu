@@ -261,6 +261,7 @@ extern "C" int gpu_ContextSetOptions(gpu_Context* ctx, const lobpcg_gpu_options*
 {
   if (opt->precision != LOBPCG_GPU_FP64 && opt->precision != LOBPCG_GPU_MIXED)
     return gb_fail(ctx, "unknown precision mode %d", opt->precision);
+  if (opt->wait_polls < 0) return gb_fail(ctx, "wait_polls must be >= 0 (0 = default)");
   ctx->opt = *opt;
   return 0;
 }

@@ -743,6 +743,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
   }
   int comp = 0;
   int split_undos = 0; /* consecutive undone steps in split mode */
+  int timed_out = 0;   /* a tensor-core kernel reported a timed-out wait */
   for (int i = 0; i < k; i++) prev_act[i] = i;  /* phase_setup left R for all columns */
   gb_mv_set_mask_host(X, NULL);
   gb_mv_set_mask_host(AX, NULL);
@@ -1133,6 +1134,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         /* a tensor-core kernel gave up waiting: its output is incomplete */
         tc_ok = 0;
         undo = 1;
+        timed_out = 1;
       }
     }
     if (!undo) {
@@ -1184,7 +1186,7 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
         haveP = 0;
       } else if (!tc_ok || comp) {
         ctl->handed_over = 1;
-        s->ctx->stats.handover_reason = 5;
+        s->ctx->stats.handover_reason = timed_out ? 6 : 5;
         break;
       }
       comp = 1;
@@ -1208,6 +1210,17 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       dump_lambda(s->h_norm, s->h_lam, *it, k);
     } else if (s->verbosity == 1) {
       printf("Iteration %d \tbsize %d \tmaxres %22.14e\n", *it, nR, max_value(s->h_norm, k));
+    }
+  }
+  /* a tensor-core kernel that gave up waiting leaves NaN in its output, which
+     the checks above may have met first (a block that is not definite, a
+     failed Rayleigh-Ritz solve): the error word names the cause */
+  if (tc_ok && ctl->handed_over) {
+    int derr = 0;
+    if (gb_device_error(s->ctx, &derr)) return -2;
+    if (derr) {
+      s->ctx->stats.device_errors++;
+      s->ctx->stats.handover_reason = 6;
     }
   }
   /* the FP64 block goes straight to the caller's block */

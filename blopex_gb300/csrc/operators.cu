@@ -415,7 +415,6 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
   __shared__ __align__(128) float ring[ST7T_DEPTH * ST7T_SLOT];
   __shared__ __align__(8) uint64_t bar[ST7T_DEPTH];
   __shared__ int abort_flag;
-  __shared__ int never_flag;
   const int t = threadIdx.x, tx = t & 31, ty = t >> 5;
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + 31) / 32;
   const long b = blockIdx.x;
@@ -425,7 +424,6 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
   const long plane = (long)nx * ny;
   if (t == 0) {
     abort_flag = 0;
-    never_flag = 0;
     for (int q = 0; q < ST7T_DEPTH; q++) mbar_init(&bar[q], 1);
   }
   fence_proxy_async();
@@ -523,7 +521,7 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
     atomicExch(err, 1);
     // copies issued but not seen landing: wait for them before the CTA exits
     for (int c = waited; c < issued; c++)
-      mbar_wait(&bar[c % ST7T_DEPTH], (uint32_t)((c / ST7T_DEPTH) & 1), &never_flag);
+      mbar_drain(&bar[c % ST7T_DEPTH], (uint32_t)((c / ST7T_DEPTH) & 1));
   }
 }
 
@@ -957,6 +955,8 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
       else if (f32 && st7t_maps(op, X, &tmc, &tmz) == 0) {
         st7t_cols pc;
         for (int c = 0; c < w; c++) pc.c[c] = X->active[c];
+        if (tc_apply_wait_polls(ctx->opt.wait_polls, S(ctx)) != cudaSuccess)
+          return gb_fail(ctx, "stencil7: cannot set the wait limit");
         st7_tma_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
                          0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1], op->c32[2],
                                       (float)op->shift, tmc, tmz, pc, yc, w, ctx->dcount + 5);

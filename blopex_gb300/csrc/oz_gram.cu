@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   unsigned char* adig = smem + 2 * OZG_RAW;    // [S][128 rows][128 B]
   __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag, never_flag;
+  __shared__ int abort_flag;
   __shared__ __align__(16) int part[1024];  // per (column, 8-row group) largest exponent
   // this tile's column pointers and kinds (0 absent, 1 FP32, 2 FP64) in shared
   // memory: a runtime index into the kernel-parameter table is slow
@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   }
   if (tid == 0) {
     abort_flag = 0;
-    never_flag = 0;
     for (int s = 0; s < 2; s++) {
       mbar_init(&raw_full[s], 1);
       mbar_init(&raw_empty[s], OZG_NPROD);
@@ -181,7 +180,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
     }
     // no copy may still be landing when the CTA exits
     for (int s = 0; s < 2; s++)
-      if (issued[s] > 0) mbar_wait(&raw_full[s], (uint32_t)(((issued[s] - 1) >> 1) & 1), &never_flag);
+      if (issued[s] > 0) mbar_drain(&raw_full[s], (uint32_t)(((issued[s] - 1) >> 1) & 1));
   } else if (warp == 2 || warp == 3 || warp >= 12) {
     // ------------------------------------------------------- digit slices
     // (every producer runs every iteration: the named barrier below must be
@@ -374,7 +373,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   // TMEM is freed only after the last MMA has completed and every epilogue
   // read has finished
   if (warp == 0) {
-    mbar_wait(&done_bar, 0, &never_flag);
+    mbar_drain(&done_bar, 0);
     __syncwarp();
   }
   tc_fence_before();
@@ -392,8 +391,11 @@ struct ozg_offsets {
 };
 
 __global__ void oz_gram_reduce_kernel(const double* __restrict__ partial, int gx, int h, int nq,
-                                      ozg_offsets qoff, int wtot, double* G, int ldg, const int* err)
+                                      ozg_offsets qoff, int wtot, double* G, int ldg, const int* err,
+                                      int* status)
 {
+  // a timed-out wait is also reported through the context's device error word
+  if (blockIdx.x == 0 && threadIdx.x == 0 && *err) *status = *err;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= h * wtot) return;
   const int i = e % h, col = e / h;
@@ -457,13 +459,15 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
   if (cudaFuncSetAttribute(oz_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZG_SMEM) !=
       cudaSuccess)
     return gb_fail(ctx, "oz_gram: cannot reserve %d bytes of shared memory", OZG_SMEM);
+  if (tc_apply_wait_polls(ctx->opt.wait_polls, (cudaStream_t)ctx->stream) != cudaSuccess)
+    return gb_fail(ctx, "oz_gram: cannot set the wait limit");
   gb_prof_rec pr;
   gb_prof_begin(ctx, &pr, GB_K_OZ_GRAM);
   oz_gram_kernel<<<dim3((unsigned)gx, (unsigned)ntiles), OZG_THREADS, OZG_SMEM, (cudaStream_t)ctx->stream>>>(prm);
   int rc = gb_cuda_check(ctx, (int)cudaGetLastError(), "oz_gram");
   if (rc) return rc;
   oz_gram_reduce_kernel<<<(h * wtot + 255) / 256, 256, 0, (cudaStream_t)ctx->stream>>>(
-      prm.partial, (int)gx, h, nq, qoff, wtot, G, ldg, prm.err);
+      prm.partial, (int)gx, h, nq, qoff, wtot, G, ldg, prm.err, ctx->dcount + 5);
   double bytes = (ldt == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * h;
   for (int q = 0; q < nq; q++) bytes += (qdt[q] == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * qw[q];
   gb_prof_end(ctx, &pr, bytes, 2.0 * n * h * wtot);
@@ -503,6 +507,9 @@ extern "C" int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, do
   double* hbuf = (double*)malloc(sizeof(double) * (size_t)h * wtot);
   if (!rc && !hbuf) rc = gb_fail(ctx, "SplitGram: out of host memory");
   if (!rc) rc = gb_memcpy_d2h(ctx, hbuf, d, sizeof(double) * (size_t)h * wtot);
+  int err = 0;
+  if (!rc) rc = gb_device_error(ctx, &err);
+  if (!rc && err) rc = gb_fail(ctx, "SplitGram: tensor-core kernel timed out (code %d)", err);
   if (!rc)
     for (int j = 0; j < wtot; j++)
       for (int i = 0; i < h; i++) G_host[i + (size_t)j * ldg] = hbuf[i + (size_t)j * h];

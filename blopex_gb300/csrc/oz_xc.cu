@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
   double* raw = (double*)(adig + OZX_A_BYTES);   // [64 columns][128 rows]
   __shared__ uint64_t raw_full, raw_empty, a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag, never_flag;
+  __shared__ int abort_flag;
   __shared__ int colexp[64];
   __shared__ int rowexp[4][128];   // by tile modulo 4 (read by the epilogue)
   __shared__ int rowpart[8][128];  // per (8-column group, row) largest exponent
@@ -125,7 +125,6 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
 
   if (tid == 0) {
     abort_flag = 0;
-    never_flag = 0;
     mbar_init(&raw_full, 1);
     mbar_init(&raw_empty, OZX_NPROD);
     mbar_init(&a_full, OZX_NPROD);
@@ -227,7 +226,7 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
       }
     }
     // no copy may still be landing when the CTA exits
-    if (issued > 0) mbar_wait(&raw_full, (uint32_t)((issued - 1) & 1), &never_flag);
+    if (issued > 0) mbar_drain(&raw_full, (uint32_t)((issued - 1) & 1));
   } else if (warp == 2 || warp == 3 || warp >= 12) {
     // ------------------------------------------------------- digit slices
     // (every producer runs every iteration: the named barriers below must
@@ -394,7 +393,7 @@ __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_cons
   // TMEM is freed only after the last MMA has completed (done_bar is always
   // committed by the issuer) and every epilogue read has finished
   if (warp == 0) {
-    mbar_wait(&done_bar, 0, &never_flag);
+    mbar_drain(&done_bar, 0);
     __syncwarp();
   }
   tc_fence_before();
@@ -410,6 +409,8 @@ static int ozx_launch(gpu_Context* ctx, const ozx_params& prm, int nctas)
   if (cudaFuncSetAttribute(oz_xc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZX_SMEM) !=
       cudaSuccess)
     return gb_fail(ctx, "oz_xc: cannot reserve %d bytes of shared memory", OZX_SMEM);
+  if (tc_apply_wait_polls(ctx->opt.wait_polls, (cudaStream_t)ctx->stream) != cudaSuccess)
+    return gb_fail(ctx, "oz_xc: cannot set the wait limit");
   oz_xc_kernel<<<nctas, OZX_THREADS, OZX_SMEM, (cudaStream_t)ctx->stream>>>(prm);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "oz_xc");
 }

@@ -6,7 +6,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define TC_WAIT_LIMIT (1L << 24)  // polls of one bounded mbarrier wait
+#define TC_WAIT_LIMIT (1L << 24)  // polls of one bounded mbarrier wait (default)
+
+// The pipeline waits' poll limit, one copy per translation unit (no
+// relocatable device code): tc_apply_wait_polls brings it in line with the
+// launching context's option before each launch.  The drains (copies in
+// flight, the issuer's final commit before TMEM is freed) always use
+// TC_WAIT_LIMIT, so a short limit cannot let a CTA exit with work in flight.
+static __constant__ long tc_wait_polls = TC_WAIT_LIMIT;
+static long tc_wait_polls_host = TC_WAIT_LIMIT;  // the value last written to tc_wait_polls
+
+static inline cudaError_t tc_apply_wait_polls(int polls, cudaStream_t stream)
+{
+  const long v = polls > 0 ? (long)polls : TC_WAIT_LIMIT;
+  if (v == tc_wait_polls_host) return cudaSuccess;
+  // a pageable source is staged before the call returns
+  const cudaError_t e =
+      cudaMemcpyToSymbolAsync(tc_wait_polls, &v, sizeof v, 0, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) tc_wait_polls_host = v;
+  return e;
+}
 
 static __device__ __forceinline__ uint32_t smem_u32(const void* p)
 {
@@ -24,21 +43,38 @@ static __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
                : "memory");
 }
 
-// bounded wait for the phase with the given parity; false on timeout/abort
+static __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity)
+{
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// bounded pipeline wait for the phase with the given parity (tc_wait_polls
+// polls); false on timeout or when another role has aborted
 static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
 {
   const uint32_t addr = smem_u32(bar);
-  for (long i = 0; i < TC_WAIT_LIMIT; i++) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
+  const long limit = tc_wait_polls;
+  for (long i = 0; i < limit; i++) {
+    if (mbar_try_wait(addr, parity)) return true;
     if (*abort_flag) return false;
   }
+  return false;
+}
+
+// bounded drain: wait for work already in flight (copies landing in this
+// CTA's shared memory, the MMAs before TMEM is freed); never aborted early
+static __device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity)
+{
+  const uint32_t addr = smem_u32(bar);
+  for (long i = 0; i < TC_WAIT_LIMIT; i++)
+    if (mbar_try_wait(addr, parity)) return true;
   return false;
 }
 

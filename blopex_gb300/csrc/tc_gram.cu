@@ -85,7 +85,6 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) tc_gram_kernel(const __grid_co
   __shared__ uint64_t full_bar[C::NSTAGE], empty_bar[C::NSTAGE], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ int never_flag;  // the final MMA barrier is waited for even after an abort
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long r_begin = (long)blockIdx.x * prm.rows_per_cta;
@@ -94,7 +93,6 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) tc_gram_kernel(const __grid_co
 
   if (tid == 0) {
     abort_flag = 0;
-    never_flag = 0;
     for (int s = 0; s < C::NSTAGE; s++) {
       mbar_init(&full_bar[s], TCG_PRODUCERS);
       mbar_init(&empty_bar[s], 1);
@@ -230,7 +228,7 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) tc_gram_kernel(const __grid_co
   if (warp >= 4) {
     // the issuer always commits done_bar after its last MMA, so this wait
     // also guarantees no MMA is in flight when TMEM is read and freed
-    const bool ok = mbar_wait(&done_bar, 0, &never_flag) && !abort_flag;
+    const bool ok = mbar_drain(&done_bar, 0) && !abort_flag;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int quarter = warp - 4;  // TMEM lanes 32*quarter .. +31
     float* out = prm.partial + (size_t)blockIdx.x * C::USED_COLS * 128;
@@ -302,8 +300,10 @@ __device__ __forceinline__ int tcg_locate(int which, int pi, int pj, int KP, int
 
 __global__ void tc_gram_reduce_kernel(const float* __restrict__ partial, int nctas, int used_cols,
                                       int KP, int k, int nR, int nP, double* G, double* H, int ld,
-                                      const int* err)
+                                      const int* err, int* status)
 {
+  // a timed-out wait is also reported through the context's device error word
+  if (blockIdx.x == 0 && threadIdx.x == 0 && *err) *status = *err;
   const int m = k + nR + nP;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= 2 * m * m) return;
@@ -328,6 +328,8 @@ static int tc_launch(gpu_Context* ctx, long n, tcg_params* prm, int nctas)
   if (cudaFuncSetAttribute(tc_gram_kernel<KP, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return gb_fail(ctx, "tc_gram: cannot reserve %zu bytes of shared memory", smem);
+  if (tc_apply_wait_polls(ctx->opt.wait_polls, (cudaStream_t)ctx->stream) != cudaSuccess)
+    return gb_fail(ctx, "tc_gram: cannot set the wait limit");
   tc_gram_kernel<KP, COMP><<<nctas, TCG_THREADS, smem, (cudaStream_t)ctx->stream>>>(*prm);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "tc_gram");
 }
@@ -380,7 +382,7 @@ extern "C" int gb_tc_gram(gpu_Context* ctx, long n, const blk_cols* X, int k, co
   if (rc) return rc;
   const int m = k + nR + nP;
   tc_gram_reduce_kernel<<<(2 * m * m + 255) / 256, 256, 0, (cudaStream_t)ctx->stream>>>(
-      prm.partial, (int)nctas, used, KP, k, nR, nP, G, H, ld, prm.err);
+      prm.partial, (int)nctas, used, KP, k, nR, nP, G, H, ld, prm.err, ctx->dcount + 5);
   const double bytes = 4.0 * n * 2.0 * (k + nR + nP);
   const double flops = 2.0 * 2.0 * n * (double)m * m * (compensated ? 3.0 : 1.0);
   gb_prof_end(ctx, &pr, bytes, flops);

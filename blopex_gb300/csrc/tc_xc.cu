@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(TCX_THREADS, 1) tc_xc_kernel(const __grid_cons
   unsigned char* raws = stages + TCX_NSTAGE * G::STAGE;  // [slot][32 cols][128 rows] FP32
   __shared__ uint64_t full_bar[TCX_NSTAGE], empty_bar[TCX_NSTAGE], accf[2], acce[2], done_bar;
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag, never_flag;
+  __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int KB = (prm.h + 31) >> 5;
@@ -93,7 +93,6 @@ __global__ void __launch_bounds__(TCX_THREADS, 1) tc_xc_kernel(const __grid_cons
 
   if (tid == 0) {
     abort_flag = 0;
-    never_flag = 0;
     for (int s = 0; s < TCX_NSTAGE; s++) {
       mbar_init(&full_bar[s], TCX_NPROD);
       mbar_init(&empty_bar[s], 1);
@@ -220,7 +219,8 @@ __global__ void __launch_bounds__(TCX_THREADS, 1) tc_xc_kernel(const __grid_cons
 #pragma unroll
       for (int j = 0; j < NW; j++)
         zv[j] = (prm.has_z && j < prm.w && row < prm.n) ? ((const float*)prm.z.col[j])[row] : 0.f;
-      if (!mbar_wait(&accf[buf], (uint32_t)((i >> 1) & 1), &abort_flag)) {
+      const bool got = mbar_wait(&accf[buf], (uint32_t)((i >> 1) & 1), &abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {  // tcgen05.ld needs the whole warp
         abort_flag = 1;
         atomicExch(prm.err, 4);
         break;
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(TCX_THREADS, 1) tc_xc_kernel(const __grid_cons
   // TMEM is freed only after the last MMA has completed (done_bar is always
   // committed by the issuer) and every epilogue read has finished
   if (warp == 0) {
-    mbar_wait(&done_bar, 0, &never_flag);
+    mbar_drain(&done_bar, 0);
     __syncwarp();
   }
   tc_fence_before();
@@ -266,6 +266,8 @@ static int tcx_launch(gpu_Context* ctx, const tcx_params& prm, int nctas)
   if (cudaFuncSetAttribute(tc_xc_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
       cudaSuccess)
     return gb_fail(ctx, "tc_xc: cannot reserve %d bytes of shared memory", smem);
+  if (tc_apply_wait_polls(ctx->opt.wait_polls, (cudaStream_t)ctx->stream) != cudaSuccess)
+    return gb_fail(ctx, "tc_xc: cannot set the wait limit");
   tc_xc_kernel<NW><<<nctas, TCX_THREADS, smem, (cudaStream_t)ctx->stream>>>(prm);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "tc_xc");
 }
@@ -324,6 +326,12 @@ extern "C" int gb_device_error(gpu_Context* ctx, int* err)
   if (*h && cudaMemsetAsync(ctx->dcount + 5, 0, sizeof(int), (cudaStream_t)ctx->stream) != cudaSuccess)
     return gb_fail(ctx, "device error word: memset failed");
   return 0;
+}
+
+extern "C" int gpu_ContextDeviceError(gpu_Context* ctx, int* code)
+{
+  *code = 0;
+  return gb_device_error(ctx, code);
 }
 
 // ------------------------------------------------------- C-ABI entry point

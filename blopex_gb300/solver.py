@@ -90,6 +90,14 @@ class Context:
         msg = self.lib.gpu_ContextLastError(self.handle)
         return msg.decode() if msg else ""
 
+    def device_error(self) -> int:
+        """The device error word (read and cleared): nonzero when a tcgen05 /
+        TMA kernel gave up a bounded wait since the last read."""
+        code = ctypes.c_int(0)
+        if self.lib.gpu_ContextDeviceError(self.handle, ctypes.byref(code)):
+            raise GpuError(self.last_error())
+        return code.value
+
     def synchronize(self) -> None:
         if self.lib.gpu_ContextSynchronize(self.handle):
             raise GpuError(self.last_error())

@@ -65,6 +65,10 @@ typedef struct {
                                residual FP64-accurately on the tensor cores (split-operand X C
                                updates and X' [X R P] Gram rows), so the explicit phase itself
                                iterates to the tolerance (1) */
+  int wait_polls;           /* tests: polls of one bounded pipeline wait in the tcgen05 / TMA
+                               kernels before the wait gives up (error word, NaN output or the
+                               step undone); 0 = the default 2^24.  The limit is held per
+                               process and follows the last context that launched */
 } lobpcg_gpu_options;
 
 typedef struct {
@@ -88,7 +92,8 @@ typedef struct {
   int handover_reason;      /* mixed: why the explicit phase handed over to the FP64 loop:
                                0 it did not (converged or maxit), 1 residual below fp64_below,
                                2 no progress, 3 block not definite, 4 Rayleigh-Ritz failed,
-                               5 residual jumps not repaired by undoing the step */
+                               5 residual jumps not repaired by undoing the step, 6 a
+                               tensor-core or TMA kernel gave up waiting (its output is NaN) */
   int device_errors;        /* tensor-core kernels that reported a timed-out wait */
 } lobpcg_gpu_stats;
 
@@ -121,6 +126,10 @@ int gpu_ContextKernelTimes(gpu_Context* ctx, lobpcg_gpu_kernel_time* out, int ma
 void gpu_ContextResetKernelTimes(gpu_Context* ctx);
 /* last error message of this context ("" if none) */
 const char* gpu_ContextLastError(gpu_Context* ctx);
+/* the device error word, read and cleared (waits for the context's stream):
+   *code != 0 when a tcgen05 / TMA kernel gave up a bounded wait since the
+   last read (its output holds NaN); returns nonzero on a CUDA error */
+int gpu_ContextDeviceError(gpu_Context* ctx, int* code);
 /* kernels launched by this library since it was loaded (all contexts) */
 long long gpu_KernelLaunchCount(void);
 
