@@ -143,19 +143,39 @@ int gpu_ReadMultiVector(const char* path, long* n_out, int* k_out, double** data
     fclose(fp);
     return -2;
   }
-  double* d = (double*)calloc((size_t)n * (k > 0 ? k : 1), sizeof(double));
-  if (!d) {
+  const long total = n * k;
+  // either one value per entry, or the (real, imaginary) pairs that the
+  // reference's loader reads (multi_vector.c:681-693 of the complex serial
+  // multivector), whose imaginary parts must then be zero
+  double* raw = (double*)calloc((size_t)(2 * total + 1), sizeof(double));
+  if (!raw) {
     fclose(fp);
     return -4;
   }
-  const long total = n * k;
   long j = 0;
   double v;
-  while (j < total && fscanf(fp, "%lf", &v) == 1) d[j++] = v;
+  while (j <= 2 * total && fscanf(fp, "%lf", &v) == 1) raw[j++] = v;
   fclose(fp);
-  if (j < total) {  // short file: the reference leaves the rest as initialised (zero)
+  double* d = (double*)calloc((size_t)(total > 0 ? total : 1), sizeof(double));
+  if (!d) {
+    free(raw);
+    return -4;
+  }
+  int rc = 0;
+  if (j == 2 * total && total > 0) {
+    for (long e = 0; e < total; e++) {
+      if (raw[2 * e + 1] != 0.0) rc = -5;  // a complex entry: not a real block
+      d[e] = raw[2 * e];
+    }
+  } else if (j >= total) {
+    memcpy(d, raw, sizeof(double) * (size_t)total);
+  } else {
+    rc = -2;  // short file: the reference leaves the rest as initialised (zero)
+  }
+  free(raw);
+  if (rc) {
     free(d);
-    return -2;
+    return rc;
   }
   *n_out = n;
   *k_out = k;

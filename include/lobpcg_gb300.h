@@ -252,11 +252,13 @@ int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, double* G_hos
    (blopex_tools/matlab/matlab2hypre/matlab2hypreIJ.m: header "ilower iupper
    jlower jupper", then 0-based "row col value" triples) into CSR arrays;
    multivector text "n k" + values column by column (serial_Multi_VectorLoad,
-   blopex_serial_complex/multivector/multi_vector.c:668-700, real values);
+   blopex_serial_complex/multivector/multi_vector.c:668-700): one value per
+   entry, or the loader's (real, imaginary) pairs with zero imaginary parts;
    HYPRE ParVector files <prefix>.j.i (matlab2hypreParVectors.m: row count,
    then values) into a column-major n x k array.  Arrays are malloc'ed: free
    them with gpu_FreeHost.  Return 0, -1 (a file does not open), -2 (bad or
-   short contents), -3 (index out of range), -4 (out of memory). */
+   short contents), -3 (index out of range), -4 (out of memory), -5 (a
+   nonzero imaginary part in a multivector file). */
 int gpu_ReadHypreIJ(const char* prefix, int nfiles, long* n, long* nnz, int** rowptr,
                     int** colidx, double** vals);
 int gpu_ReadMultiVector(const char* path, long* n, int* k, double** data);

@@ -1,5 +1,7 @@
 """The reference tools' file formats (HYPRE IJ / ParVector files, multivector
 text): host readers of the C ABI on CPU, device loaders on the GPU."""
+import os
+
 import numpy as np
 import pytest
 
@@ -26,6 +28,37 @@ def test_multivector_and_parvectors_roundtrip(tmp_path):
     np.testing.assert_array_equal(IO.read_multivector(str(tmp_path / "x.txt")), x)
     IO.write_hypre_parvectors(str(tmp_path / "v"), x, nfiles=3)
     np.testing.assert_allclose(IO.read_hypre_parvectors(str(tmp_path / "v"), 4, 3), x, rtol=1e-15)
+
+
+FIX = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hypre")
+
+
+def test_hand_written_reference_layout_files():
+    """Files written by hand in the layout of the reference's tools, not by
+    this package's writers: matlab2hypreIJ.m (three row partitions, the
+    first taking the remainder row -- part = [0 3 5 7] for n = 7 -- a header
+    "ilower iupper jlower jupper" per file, 0-based "row col value" lines in
+    %16.15e), matlab2hypreParVectors.m (<prefix>.j.i with the row count then
+    the values, INFO files [n part(1:p)]) and the multivector text loader
+    (blopex_serial_complex/multivector/multi_vector.c:681-693, "n k" then
+    (real, imaginary) pairs column by column)."""
+    d = np.diag([2.0, 2.5, 3.0, 3.5, 4.0, 4.5, 5.0])
+    A = d - np.eye(7, k=1) - np.eye(7, k=-1)
+    A[0, 6] = A[6, 0] = 0.3333333333333333
+    rp, ci, va = IO.read_hypre_ij(os.path.join(FIX, "A"), 3)
+    dense = np.zeros((7, 7))
+    for r in range(7):
+        dense[r, ci[rp[r]:rp[r + 1]]] = va[rp[r]:rp[r + 1]]
+    np.testing.assert_array_equal(dense, A)
+    assert rp[-1] == 21
+    V = IO.read_hypre_parvectors(os.path.join(FIX, "v"), 2, 3)
+    np.testing.assert_array_equal(V[:, 0], np.arange(1, 8) * 0.125)
+    np.testing.assert_array_equal(V[:, 1], [-1.0, 0.5, 1e-3, 2.5e10, -3.75, 0.0, 1e-300])
+    ref = np.array([[1.5, 4.0], [-2.25, 5.0], [3.0e-05, 6.0]])
+    np.testing.assert_array_equal(IO.read_multivector(os.path.join(FIX, "x_pairs.txt")), ref)
+    np.testing.assert_array_equal(IO.read_multivector(os.path.join(FIX, "x_real.txt")), ref)
+    with pytest.raises(OSError, match=r"\(-5\)"):
+        IO.read_multivector(os.path.join(FIX, "x_complex.txt"))
 
 
 def test_reader_errors(tmp_path):
