@@ -50,6 +50,14 @@ CONFIGS = {
                label="2D 5-point diffusion 512^2, c = exp(theta), theta GRF (length 0.1, seed 3), "
                      "k=8, loss = sum(lambda) + (x_1'v)^2, d loss / d theta; FP64, tol 1e-8, "
                      "preconditioner 20 Jacobi-CG steps on A"),
+    # generalized problem with gradients in the A weights and the B diagonal
+    "c5": dict(kind="gen27", grid=(100, 100, 100), k=128, seed=4, mass_seed=14, shift=0.5,
+               tol=1e-8, maxit=1000, inner_cg=20, adjoint_tol=1e-8,
+               label="generalized A x = lambda B x: 27-point graph Laplacian 100^3 (n=1000000), "
+                     "edge weights U[0.5,1.5] seed 4, shift 0.5; B = diag(U[0.5,1.5] seed 14); "
+                     "k=128, mixed precision, tol 1e-8, preconditioner 20 Jacobi-CG steps on A; "
+                     "loss = sum(lambda) + (x_1'v)^2, gradient w.r.t. the 13 n edge weights and "
+                     "the n entries of B"),
     # the metric's own configuration: time to k eigenpairs at residual 1e-8,
     # mixed precision against the plain FP64 GPU path
     "c3": dict(kind="stencil7", grid=(256, 256, 256), k=64, seed=2, tol=1e-8, maxit=1000,
@@ -370,6 +378,120 @@ def run_adjoint(args, cfg):
         dist.destroy_process_group()
 
 
+def run_generalized(args, cfg):
+    """--config c5: forward solve of the generalized problem in mixed
+    precision and in FP64 (same X0), then the reverse-mode gradient of the
+    loss w.r.t. the A edge weights and the B diagonal through the adjoint
+    module, from the mixed result.  value = mixed forward + backward ms; the
+    FP64 forward, the eigenvalue error and the largest B-subspace angle of
+    the mixed eigenvectors against the FP64 ones are reported beside."""
+    import torch
+    from blopex_gb300 import adjoint as AD
+    from blopex_gb300 import problems as P
+    from blopex_gb300 import solver as S
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    nx, ny, nz = cfg["grid"]
+    n, k = nx * ny * nz, cfg["k"]
+    w = P.stencil27_weights(nx, ny, nz, seed=cfg["seed"])
+    bdiag = P.mass_diagonal(n, seed=cfg["mass_seed"])
+    v = np.random.default_rng(cfg["seed"]).standard_normal(n)
+    v /= np.linalg.norm(v)
+    ctx = S.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    A = S.Stencil27(ctx, nx, ny, nz, w, cfg["shift"])
+    B = S.Diagonal(ctx, bdiag)
+    J = S.Diagonal(ctx, 1.0 / A.diagonal())
+    T = S.PCGPreconditioner(ctx, A, J, cfg["inner_cg"])
+    glam = np.ones(k)
+    maxit = args.maxit or cfg["maxit"]
+
+    def timed(f, *a):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        out = f(*a)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    def forward(X, mode):
+        X.set_random(cfg["seed"])
+        ctx.set_options(precision=S.MIXED if mode == "mixed" else S.FP64)
+        return S.lobpcg_solve_double(X, A, B=B, T=T, atol=cfg["tol"], rtol=1e-50, maxit=maxit,
+                                     history=False)
+
+    def backward(X, r):
+        x1 = X.to_host()[:, 0]
+        G = np.zeros((n, k), order="F")
+        G[:, 0] = 2.0 * (x1 @ v) * v
+        adj = AD.eigenvector_adjoint(X, r.lam, A, G=G, glam=glam, B=B, T=T,
+                                     tol=cfg["adjoint_tol"], maxit=20000)
+        return adj, AD.operator_gradient(A, X, adj.W), AD.mass_gradient(B, X, adj.W, r.lam, adj.xg)
+
+    Xm, Xf = S.MultiVector(ctx, n, k), S.MultiVector(ctx, n, k)
+    for _ in range(args.warmup):
+        forward(Xm, "mixed")
+    ctx.profiling(True)
+    ctx.reset_kernel_times()
+    sampler = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    sampler.start()
+    launches0 = ctx.lib.gpu_KernelLaunchCount()
+    fwd, bwd = [], []
+    for _ in range(args.steps):
+        rm, tf = timed(forward, Xm, "mixed")
+        st_m = dict(rm.stats)
+        (adj, ga, gb), tb = timed(backward, Xm, rm)
+        fwd.append(tf)
+        bwd.append(tb)
+    launches = ctx.lib.gpu_KernelLaunchCount() - launches0
+    clocks = sampler.stop()
+    kt = ctx.kernel_times()
+    ctx.profiling(False)
+    rf, tf64 = timed(forward, Xf, "fp64")
+    # eigenvalue error and the largest principal angle in the B inner product
+    xm, xf = Xm.to_host(), Xf.to_host()
+    d = xm - xf @ (xf.T @ (bdiag[:, None] * xm))
+    dd = d.T @ (bdiag[:, None] * d)
+    sin_max = float(np.sqrt(max(np.linalg.eigvalsh(0.5 * (dd + dd.T))[-1], 0.0)))
+    xbx = xm.T @ (bdiag[:, None] * xm)
+    tf_ = max_over_ranks(statistics.median(fwd), dist, "cuda")
+    tb_ = max_over_ranks(statistics.median(bwd), dist, "cuda")
+    total = sum(v_["ms"] for v_ in kt.values()) or 1.0
+    line = {"metric": "fwd+bwd ms (mixed-precision generalized solve + reverse-mode gradient)",
+            "value": tf_ + tb_, "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tf_ + tb_, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 mixed", "data": "synthetic",
+            "config": {"workload": cfg["label"], "n": n, "k": k, "tol": cfg["tol"],
+                       "maxit": maxit, "adjoint_tol": cfg["adjoint_tol"],
+                       "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (X alone is n*k*8 = 1.02 GB)"},
+            "forward_ms": tf_, "backward_ms": tb_, "fwd_plus_bwd_over_fwd": (tf_ + tb_) / tf_,
+            "mixed": arm_summary(rm, tf_ / 1e3) | {"stats": {
+                kk: st_m[kk] for kk in ("iterations_fp32", "iterations_fp64", "handover_reason",
+                                        "explicit_undos", "explicit_p_drops")}},
+            "fp64": arm_summary(rf, tf64 / 1e3),
+            "mixed_over_fp64_forward_speedup": tf64 / tf_,
+            "max_rel_lambda_error_vs_fp64": float(np.max(np.abs(rm.lam - rf.lam) / np.abs(rf.lam))),
+            "largest_subspace_angle_rad": float(np.arcsin(min(sin_max, 1.0))),
+            "orthonormality_xtbx_minus_i_fro": float(np.linalg.norm(xbx - np.eye(k))),
+            "adjoint_cg_iterations": adj.iterations,
+            "adjoint_max_rel_residual": adj.max_rel_residual,
+            "gradient_norms": {"a_weights": float(np.linalg.norm(ga)),
+                               "b_diagonal": float(np.linalg.norm(gb))},
+            "kernels": {nm: {"share": x["ms"] / total, "launches": x["launches"],
+                             "avg_ms": x["ms"] / x["launches"]}
+                        for nm, x in sorted(kt.items(), key=lambda kv: -kv[1]["ms"])[:10]},
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_reference(args, cfg):
     """--impl reference: the CPU implementation of the path timed alone."""
     rank = int(os.environ.get("RANK", "0"))
@@ -467,7 +589,7 @@ def main():
         cfg["label"] += f" [profiling case: grid {args.grid}^3]"
 
     if args.impl == "reference":
-        if cfg["kind"] == "adjoint5":
+        if cfg["kind"] in ("adjoint5", "gen27"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no "
                               "derivatives (no adjoint or gradient of its eigenpairs)"}), flush=True)
             return
@@ -475,6 +597,9 @@ def main():
         return
     if cfg["kind"] == "adjoint5":
         run_adjoint(args, cfg)
+        return
+    if cfg["kind"] == "gen27":
+        run_generalized(args, cfg)
         return
 
     import torch
