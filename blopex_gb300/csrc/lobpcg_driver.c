@@ -820,11 +820,10 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       for (int i = 0; i < k; i++) lg += log(s->h_norm[i] + DBL_MIN);
       lg /= k;
       /* split mode has no FP32 floor to detect: its residuals plateau as
-         long as the FP64 loop's do (minutes on a 256^3 problem), so only a
-         long stretch without progress -- shorter near the tolerance, where a
-         precision floor would show -- hands over */
-      const int limit = !split ? ctl->stall_limit
-                        : (mx < 100.0 * s->tol.absolute ? 30 : 5 * ctl->stall_limit);
+         long as the FP64 loop's do (near the tolerance LOBPCG itself stalls
+         for tens of iterations on a 256^3 problem), so only a long stretch
+         without progress hands over */
+      const int limit = !split ? ctl->stall_limit : 5 * ctl->stall_limit;
       if (lg < best - 1e-3) {
         best = lg;
         stall = 0;

@@ -13,6 +13,9 @@ environment variable BLOPEX_REFERENCE_DIR):
     python tests/golden/make_golden.py --large    # the 128^3 cases (hours
                                                   # of CPU; the three builds
                                                   # run in parallel processes)
+    python tests/golden/make_golden.py --fingerprints  # add the input
+                                                  # fingerprints to existing
+                                                  # 128^3 fixtures
 """
 from __future__ import annotations
 
@@ -34,6 +37,16 @@ from tests.golden import cases as C  # noqa: E402
 
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def fingerprint(a: np.ndarray) -> list:
+    """Two weighted sums of a floating-point input: they pin it to rounding
+    where its SHA-256 cannot -- numpy's exp() differs in the last bit between
+    x86-64 and aarch64, so exp(N(0,1)) coefficients regenerated on another
+    host hash differently while agreeing to ~1e-16."""
+    v = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    w = (np.arange(v.size) % 97 + 1.0) / 97.0
+    return [float(np.sum(v)), float(np.dot(v, w))]
 
 
 def capture_stdout(fn):
@@ -123,6 +136,8 @@ def main_large(names):
                                                       "lambda_hist", "res_hist")})
             out["reference_seconds_one_core"] = plain["seconds"]
             out["inputs_sha256"] = {key: sha(val) for key, val in case.arrays().items()}
+            out["inputs_fingerprint"] = {key: fingerprint(val) for key, val in case.arrays().items()
+                                         if np.asarray(val).dtype.kind == "f"}
             out["variants"] = {}
             for v in ("fma", "x87"):
                 rv = jobs[(name, v)].result()
@@ -135,7 +150,29 @@ def main_large(names):
                   f"({plain['seconds']:.0f} s)", flush=True)
 
 
+def add_fingerprints(names):
+    """Add the input fingerprints to existing large fixtures, after checking
+    that the regenerated inputs are those the fixture was made from."""
+    for name in names:
+        path = os.path.join(HERE, f"{name}.json")
+        with open(path) as f:
+            g = json.load(f)
+        case = C.build(name)
+        arrays = case.arrays()
+        for key, val in arrays.items():
+            if sha(val) != g["inputs_sha256"][key]:
+                raise SystemExit(f"{name}: input {key} differs from the fixture's")
+        g["inputs_fingerprint"] = {key: fingerprint(val) for key, val in arrays.items()
+                                   if np.asarray(val).dtype.kind == "f"}
+        with open(path, "w") as f:
+            json.dump(g, f, indent=0)
+        print(f"{name}: fingerprints added", flush=True)
+
+
 def main():
+    if "--fingerprints" in sys.argv:
+        add_fingerprints(C.LARGE_NAMES)
+        return
     if not O.have_ref():
         O.build(ref=True)
     O.build_ref_variants()
