@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include "internal.h"
+#include "blas32.cuh"
 
 #define CUDA_LAUNCH_CHECK(ctx, what) gb_cuda_check((ctx), (int)cudaGetLastError(), (what))
 
@@ -498,6 +499,47 @@ __global__ void dot_reduce_kernel(const double* __restrict__ partial, int nb, id
   out[idx.v[j]] = s;
 }
 
+// FP32 blocks with 16-byte aligned columns: float4 loads, exact products in
+// a compensated FP32 sum flushed to FP64 every 64 terms (blas32.cuh)
+__global__ void __launch_bounds__(256) dot32_partial_kernel(blk_cols X, blk_cols Y, long n,
+                                                            double* __restrict__ partial)
+{
+  const float4* x = (const float4*)X.col[blockIdx.y];
+  const float4* y = (const float4*)Y.col[blockIdx.y];
+  const long n4 = n >> 2, stride = (long)gridDim.x * blockDim.x;
+  double acc = 0.0;
+  float s = 0.f, c = 0.f;
+  int cnt = 0;
+#pragma unroll 4
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < n4; v += stride) {
+    acc_prod32x4(s, c, x[v], y[v]);
+    if (++cnt == 16) {
+      acc += (double)s + (double)c;
+      s = c = 0.f;
+      cnt = 0;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {  // the last n % 4 rows
+    const long r = 4 * n4 + threadIdx.x;
+    acc_prod32(s, c, ((const float*)x)[r], ((const float*)y)[r]);
+  }
+  acc += (double)s + (double)c;
+  const double t = block_sum256(acc);
+  if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+}
+
+extern "C" int gb_dot_reduce(gpu_Context* ctx, const double* partial, int nb, int w, double* out,
+                             const int* idx)
+{
+  idx_table t;
+  fill_idx(&t, idx, w);
+  dot_reduce_kernel<<<(w + 63) / 64, 64, 0, S(ctx)>>>(partial, nb, t, w, out);
+  gb_count_launch(1);
+  return CUDA_LAUNCH_CHECK(ctx, "dot_reduce");
+}
+
+extern "C" unsigned gb_row_blocks(gpu_Context* ctx, long n, int w) { return row_blocks(ctx, n, w); }
+
 extern "C" int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X,
                            const blk_cols* Y, int w, double* out, const int* idx)
 {
@@ -512,6 +554,8 @@ extern "C" int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* 
   gb_prof_begin(ctx, &pr, GB_K_BLAS1);
   if (dtype == GPU_MV_FLOAT64)
     dot_partial_kernel<double><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n, partial);
+  else if (cols_aligned16(X->col, w) && cols_aligned16(Y->col, w))
+    dot32_partial_kernel<<<grid, 256, 0, S(ctx)>>>(*X, *Y, n, partial);
   else
     dot_partial_kernel<float><<<grid, 256, 0, S(ctx)>>>(*X, *Y, n, partial);
   dot_reduce_kernel<<<(w + 63) / 64, 64, 0, S(ctx)>>>(partial, nb, t, w, out);

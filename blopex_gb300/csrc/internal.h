@@ -131,6 +131,11 @@ int gb_scale_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X, const 
 /* out[idx[j]] = X(:,j)' Y(:,j) (FP64 device) */
 int gb_dot_cols(gpu_Context* ctx, int dtype, long n, const blk_cols* X, const blk_cols* Y, int w,
                 double* out, const int* idx);
+/* the fixed-order sum of per-CTA partials partial[j * nb + b] into
+   out[idx[j]], and the row-block count the column kernels use */
+int gb_dot_reduce(gpu_Context* ctx, const double* partial, int nb, int w, double* out,
+                  const int* idx);
+unsigned gb_row_blocks(gpu_Context* ctx, long n, int w);
 /* Y(:,j) (dtype_y) = X(:,j) (dtype_x), converting precision */
 int gb_convert(gpu_Context* ctx, long n, int dtype_x, const blk_cols* X, int dtype_y,
                const blk_cols* Y, int w);

@@ -158,3 +158,87 @@ def test_operator_diagonal(ctx):
             e[i] = 1
             d[i] = O.apply(oop, e)[i, 0]
         np.testing.assert_allclose(gop.diagonal(), d, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("n", [1, 5, 4099, 1000003])
+def test_fp32_dot_products_fp64_accurate(ctx, n):
+    """Column inner products of FP32 blocks (mv_MultiVectorByMultiVectorDiag,
+    blockops.cu's FP32 path): exact products in a compensated FP32 sum
+    flushed to FP64, so |error| <= 1e-12 sum |x_i y_i| although the data are
+    FP32 and no FP64 arithmetic runs per element."""
+    rng = np.random.default_rng(n)
+    k = 7
+    x = rng.standard_normal((n, k)).astype(np.float32).astype(np.float64)
+    y = (rng.standard_normal((n, k)) * 10.0 ** rng.uniform(-3, 3, size=(n, 1)))
+    y = y.astype(np.float32).astype(np.float64)
+    X = S.MultiVector.from_host(ctx, x, S.FLOAT32)
+    Y = S.MultiVector.from_host(ctx, y, S.FLOAT32)
+    interp = S._Interp(ctx.lib)
+    xx = ctx.lib.mv_MultiVectorWrap(interp.ptr, X.handle, 0)
+    yy = ctx.lib.mv_MultiVectorWrap(interp.ptr, Y.handle, 0)
+    d = np.zeros(k)
+    ctx.lib.mv_MultiVectorByMultiVectorDiag(xx, yy, None, k, d.ctypes.data)
+    ctx.lib.mv_MultiVectorDestroy(xx)
+    ctx.lib.mv_MultiVectorDestroy(yy)
+    assert ctx.last_error() == ""
+    ref = np.einsum("ij,ij->j", x, y)  # products exact in FP64
+    assert np.all(np.abs(d - ref) <= 1e-12 * np.einsum("ij,ij->j", np.abs(x), np.abs(y)))
+
+
+def _cg_reference(A, M, X, steps):
+    """The inner-CG recurrence of gpu_PCGPreconditionerCreate in FP64 numpy."""
+    Y = np.zeros_like(X)
+    for j in range(X.shape[1]):
+        r = X[:, j].copy()
+        z = M * r if M is not None else r.copy()
+        p = z.copy()
+        rho = r @ z
+        y = np.zeros_like(r)
+        for it in range(steps):
+            q = A @ p
+            alpha = rho / (p @ q) if rho != 0 else 0.0
+            y += alpha * p
+            r -= alpha * q
+            if it + 1 == steps:
+                break
+            z = M * r if M is not None else r
+            rho2 = r @ z
+            beta = rho2 / rho if rho != 0 else 0.0
+            p = z + beta * p
+            rho = rho2
+        Y[:, j] = y
+    return Y
+
+
+@pytest.mark.parametrize("dtype", [S.FLOAT32, S.FLOAT64])
+@pytest.mark.parametrize("jacobi", [True, False])
+@pytest.mark.parametrize("grid", [(13, 11, 7), (16, 16, 16)])
+def test_pcg_preconditioner_matches_cg(ctx, dtype, jacobi, grid):
+    """T X by the inner-CG preconditioner (FP32: the fused float4 kernels, a
+    ragged n % 4 tail included; FP64: the column kernels) against the same
+    recurrence in FP64 numpy."""
+    import scipy.sparse as sp
+    nx, ny, nz = grid
+    n, w, steps = nx * ny * nz, 5, 8
+    cx, cy, cz = P.stencil7_coefficients(nx, ny, nz, seed=7)
+    rp, ci, va = P.stencil7_to_csr(cx, cy, cz)
+    Acsr = sp.csr_matrix((va, ci, rp), shape=(n, n))
+    if dtype == S.FLOAT32:
+        # the FP32 operator and Jacobi weights, as the device applies them
+        Acsr = sp.csr_matrix((va.astype(np.float32).astype(np.float64), ci, rp), shape=(n, n))
+    M = 1.0 / P.stencil7_diagonal(cx, cy, cz)
+    A = S.Stencil7(ctx, cx, cy, cz)
+    Mop = S.Diagonal(ctx, M) if jacobi else None
+    T = S.PCGPreconditioner(ctx, A, Mop, steps)
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((n, w))
+    if dtype == S.FLOAT32:
+        x = x.astype(np.float32).astype(np.float64)
+        M = M.astype(np.float32).astype(np.float64)
+    X = S.MultiVector.from_host(ctx, x, dtype)
+    Y = S.MultiVector(ctx, n, w, dtype)
+    T.apply(X, Y)
+    ref = _cg_reference(Acsr, M if jacobi else None, x, steps)
+    tol = 1e-10 if dtype == S.FLOAT64 else 2e-4
+    err = np.linalg.norm(Y.to_host() - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    assert np.all(err <= tol), err
