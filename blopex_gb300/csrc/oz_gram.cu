@@ -93,7 +93,7 @@ static __device__ __forceinline__ void ozg_load8(const unsigned char* src, float
 __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_constant__ ozg_params prm)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* smem = smem_align1024(smem_raw);
   unsigned char* raws = smem;                  // [2][128 columns][528 B]
   unsigned char* adig = smem + 2 * OZG_RAW;    // [S][128 rows][128 B]
   __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;

@@ -99,7 +99,7 @@ static __device__ __forceinline__ void ozx_load_z(int z_kind, const void* const*
 __global__ void __launch_bounds__(OZX_THREADS, 1) oz_xc_kernel(const __grid_constant__ ozx_params prm)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* smem = smem_align1024(smem_raw);
   unsigned char* cdig = smem;                    // [half][S][32 rows][128 B]
   unsigned char* adig = smem + OZX_C_BYTES;      // [S][128 rows][128 B]
   double* raw = (double*)(adig + OZX_A_BYTES);   // [64 columns][128 rows]

@@ -32,6 +32,15 @@ static __device__ __forceinline__ uint32_t smem_u32(const void* p)
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// the first 1024-byte boundary at or after p in shared memory, by pointer
+// arithmetic on p: the compiler then still sees a shared-memory pointer and
+// emits shared loads and stores through it (a round trip through an integer
+// makes every access generic, with the latency of a global access)
+static __device__ __forceinline__ unsigned char* smem_align1024(unsigned char* p)
+{
+  return p + ((1024u - (smem_u32(p) & 1023u)) & 1023u);
+}
+
 static __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
 {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");

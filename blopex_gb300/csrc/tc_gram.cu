@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(TCG_THREADS, 1) tc_gram_kernel(const __grid_co
   using C = tcg_cfg<KP, COMP>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned operand stages (SW128 atoms)
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* smem = smem_align1024(smem_raw);
   __shared__ uint64_t full_bar[C::NSTAGE], empty_bar[C::NSTAGE], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;

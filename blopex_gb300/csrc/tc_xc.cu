@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(TCX_THREADS, 1) tc_xc_kernel(const __grid_cons
 {
   using G = tcx_cfg<NW>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* smem = smem_align1024(smem_raw);
   unsigned char* cmat = smem;                         // [kb][hi, lo][NW rows][128 B]
   unsigned char* stages = smem + G::C_BYTES;          // [s][hi, lo][128 rows][128 B]
   unsigned char* raws = stages + TCX_NSTAGE * G::STAGE;  // [slot][32 cols][128 rows] FP32
