@@ -259,6 +259,55 @@ static __device__ __forceinline__ void oz_digits4_f64(double v, int E, float (&d
   oz_digits4_u((uint32_t)oz_fixed64<28>(v, E), (uint32_t)((uint64_t)__double_as_longlong(v) >> 63) << 31, d);
 }
 
+// ------------------------------------ four 8-bit digits (32 fraction bits)
+// The Gram's digits: with its 64-row chunks the level sums of 8-bit digits
+// stay exact in FP32 (|d0| <= 256, |d_t| <= 128 after, or d2 <= 256 on the
+// integer path: every level below 2^24 over 64 rows), so a fourth bit per
+// digit costs nothing and makes the products 16 times more accurate.
+//   u = v 2^(32 - (E - 1022)),  |u| < 2^32 (exact: v's 24 bits, scaled)
+//   h = rint(u / 2^16), l = u - 2^16 h
+//   d0 = rint(h / 2^8), d1 = h - 2^8 d0, d2 = rint(l / 2^8), d3 = rint(l - 2^8 d2)
+// so u ~= 2^24 d0 + 2^16 d1 + 2^8 d2 + d3 to within 1/2.
+static __device__ __forceinline__ void oz_digits4x8_hl(float h, float l, float (&d)[4])
+{
+  d[0] = fmaf(h, 0.00390625f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+  d[1] = fmaf(d[0], -256.0f, h);
+  d[2] = fmaf(l, 0.00390625f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+  d[3] = (fmaf(d[2], -256.0f, l) + OZ_RINT_MAGIC) - OZ_RINT_MAGIC;
+}
+
+// FP32 value; scale = 2^(32 - (E - 1022)) as a float
+static __device__ __forceinline__ void oz_digits4x8_f32(float v, float scale, float (&d)[4])
+{
+  const float u = v * scale;
+  const float h = fmaf(u, 0.0000152587890625f, OZ_RINT_MAGIC) - OZ_RINT_MAGIC;  // 2^-16
+  const float l = fmaf(h, -65536.0f, u);
+  oz_digits4x8_hl(h, l, d);
+}
+
+// the scale of oz_digits4x8_f32 for a group exponent E, 0 when E is outside
+// the range the float can hold (the caller then takes the integer path)
+static __device__ __forceinline__ float oz_scale4x8(int E)
+{
+  const int f = 32 + 1022 - E + 127;
+  return (f >= 1 && f <= 254) ? __uint_as_float((uint32_t)f << 23) : 0.0f;
+}
+
+// a 32-bit fixed point magnitude U (<= 2^32) with sign bit sg (bit 31): its
+// two 16-bit halves as exact floats (h <= 2^16), then the digits
+static __device__ __forceinline__ void oz_digits4x8_u(uint64_t U, uint32_t sg, float (&d)[4])
+{
+  const float h = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(U >> 16)) - 8388608.0f) ^ sg);
+  const float l = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(U & 0xFFFFu)) - 8388608.0f) ^ sg);
+  oz_digits4x8_hl(h, l, d);
+}
+
+// FP64 value: the 32-bit fixed point integer from its bits, then as above
+static __device__ __forceinline__ void oz_digits4x8_f64(double v, int E, float (&d)[4])
+{
+  oz_digits4x8_u(oz_fixed64<32>(v, E), (uint32_t)((uint64_t)__double_as_longlong(v) >> 63) << 31, d);
+}
+
 // two digits (floats holding integers) as one word of two bf16 patterns
 static __device__ __forceinline__ uint32_t oz_pack_bf16(float lo, float hi)
 {

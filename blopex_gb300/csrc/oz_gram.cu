@@ -9,9 +9,10 @@
 // while unbiased errors of 1e-7 leave its convergence that of FP64.
 //
 // The contraction runs over n rows in chunks of 64.  Within a chunk every
-// column has its own power-of-two scale and is cut into S = 4 7-bit digits
-// (28 fraction bits; FP32 arithmetic, oz_digits4_*); level L = t + u of the
-// digit products is summed exactly in FP32 in TMEM (|sum| < 2^22).  After each chunk the four
+// column has its own power-of-two scale and is cut into S = 4 8-bit digits
+// (32 fraction bits; FP32 arithmetic, oz_digits4x8_*); level L = t + u of the
+// digit products is summed exactly in FP32 in TMEM (|sum| < 2^24 over 64
+// rows: 8 bits per digit is the widest that holds).  After each chunk the four
 // levels are combined (FP32, round to nearest), scaled, and added into
 // double-float (hi + lo FP32) accumulators, so the chunk sums add without
 // bias; each CTA writes its sums in FP64 and a second kernel adds the CTAs
@@ -40,7 +41,7 @@
 #include "oz_common.cuh"
 
 #define OZG_S 4
-#define OZG_F (7 * OZG_S)
+#define OZG_F (8 * OZG_S)                // 8-bit digits (oz_digits4x8_*)
 #define OZG_THREADS 512
 #define OZG_NPROD 192
 #define OZG_ROWS 64                      // rows per chunk
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
           // first for FP64 values, or for FP32 groups whose scale leaves the
           // float range)
           float dg[8][OZG_S];
-          const float sc = oz_scale4(E);
+          const float sc = oz_scale4x8(E);
           const int nr = min(8, rows - 8 * q);
           if (kind == 1) {
             float v[8];
@@ -244,17 +245,17 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
             for (int x = 0; x < 8; x++) v[x] = x < nr ? v[x] : 0.0f;
             if (sc != 0.0f) {
 #pragma unroll
-              for (int x = 0; x < 8; x++) oz_digits4_f32(v[x], sc, dg[x]);
+              for (int x = 0; x < 8; x++) oz_digits4x8_f32(v[x], sc, dg[x]);
             } else {
 #pragma unroll
               for (int x = 0; x < 8; x++)
-                oz_digits4_u((uint32_t)oz_fixed32<OZG_F>(v[x], E), __float_as_uint(v[x]) & 0x80000000u, dg[x]);
+                oz_digits4x8_u(oz_fixed32<OZG_F>(v[x], E), __float_as_uint(v[x]) & 0x80000000u, dg[x]);
             }
           } else if (kind == 2) {
             double v[8];
             ozg_load8(raw + j * OZG_COLSTRIDE + 64 * q, v);
 #pragma unroll
-            for (int x = 0; x < 8; x++) oz_digits4_f64(x < nr ? v[x] : 0.0, E, dg[x]);
+            for (int x = 0; x < 8; x++) oz_digits4x8_f64(x < nr ? v[x] : 0.0, E, dg[x]);
           } else {
 #pragma unroll
             for (int x = 0; x < 8; x++)
@@ -326,8 +327,8 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       tc_fence_after();
       const int* ce = cexp[c & 3];
       const int ej = ce[j];
-      // 2^(E - 1022 - 7) per factor: the digit sums carry 2^-7 per factor
-      const float fj = (ej >= 903 && ej <= 1156) ? __uint_as_float((uint32_t)(ej - 1029 + 127) << 23) : 0.f;
+      // 2^(E - 1022 - 8) per factor: the digit sums carry 2^-8 per factor
+      const float fj = (ej >= 904 && ej <= 1157) ? __uint_as_float((uint32_t)(ej - 1030 + 127) << 23) : 0.f;
       const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(buf * 256 + 32 * ihalf);
 #pragma unroll
       for (int g = 0; g < 4; g++) {
@@ -341,30 +342,44 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
                 "=r"(r[L][5]), "=r"(r[L][6]), "=r"(r[L][7])
               : "r"(tl + (uint32_t)(L * 64 + 8 * g)));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        // Horner over the levels, highest first: v = sum_L S_L 2^(-7 L)
-        float v[8];
+        // levels 1.. by Horner, highest first: rest = sum_{L>=1} S_L 2^(8 - 8 L)
+        float rest[8];
 #pragma unroll
         for (int x = 0; x < 8; x++) {
-          v[x] = __uint_as_float(r[OZG_S - 1][x]);
+          rest[x] = __uint_as_float(r[OZG_S - 1][x]);
 #pragma unroll
-          for (int L = OZG_S - 2; L >= 0; L--) v[x] = fmaf(v[x], 0.0078125f, __uint_as_float(r[L][x]));
+          for (int L = OZG_S - 2; L >= 1; L--) rest[x] = fmaf(rest[x], 0.00390625f, __uint_as_float(r[L][x]));
         }
 #pragma unroll
         for (int x = 0; x < 8; x++) {
           const int ii = 8 * g + x;
           const int ei = ce[32 * ihalf + ii];
-          const float fi = (ei >= 903 && ei <= 1156) ? __uint_as_float((uint32_t)(ei - 1029 + 127) << 23) : 0.f;
-          const float y = v[x] * fj * fi;
-          // two-sum: hi + y = sum + err exactly
-          const float sum = hi[ii] + y;
-          const float bv = sum - hi[ii];
-          const float err = (hi[ii] - (sum - bv)) + (y - bv);
+          const float fi = (ei >= 904 && ei <= 1157) ? __uint_as_float((uint32_t)(ei - 1030 + 127) << 23) : 0.f;
+          const float fij = __fmul_rn(fj, fi);
+          // level 0 (an integer below 2^22) scaled exactly, added by a
+          // two-sum (hi + a = sum + err exactly; intrinsics: no contraction);
+          // the levels below it, 2^-8 smaller, into the low word
+          const float a = __fmul_rn(__uint_as_float(r[0][x]), fij);
+          const float sum = __fadd_rn(hi[ii], a);
+          const float bv = __fsub_rn(sum, hi[ii]);
+          const float err = __fadd_rn(__fsub_rn(hi[ii], __fsub_rn(sum, bv)), __fsub_rn(a, bv));
           hi[ii] = sum;
-          lo[ii] += err;
+          lo[ii] = fmaf(rest[x], __fmul_rn(fij, 0.00390625f), __fadd_rn(lo[ii], err));
         }
       }
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
+      // every 8 chunks: (hi, lo) <- two-sum(hi, lo), so the low word stays
+      // small and its own FP32 roundings negligible
+      if ((c & 7) == 7) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const float sum = __fadd_rn(hi[i], lo[i]);
+          const float bv = __fsub_rn(sum, hi[i]);
+          lo[i] = __fadd_rn(__fsub_rn(hi[i], __fsub_rn(sum, bv)), __fsub_rn(lo[i], bv));
+          hi[i] = sum;
+        }
+      }
     }
     double* out = prm.partial + ((size_t)b * gridDim.x + blockIdx.x) * 128 * 64 + (size_t)j * 64 + 32 * ihalf;
 #pragma unroll

@@ -7,8 +7,10 @@ every column of C into 6 digits of 7 bits (42 fraction bits below the row's /
 column's power-of-two scale) and drops the digit products below level 6, so
 |Y - XC| <= h * 2^-38 * rowmax|X| * colmax|C| (plus the rounding of the one
 final FP64 result).  The Gram cuts each column of each 64-row chunk into 4
-digits (28 fraction bits), so |G - L'Q| <= 2^-26 * sum over chunks of
-64 * max|L_i| * max|Q_j| on the chunk.  Integer-valued inputs split without
+digits of 8 bits (32 fraction bits), so the truncation is at most 2^-29 *
+64 * max|L_i| * max|Q_j| per chunk; the chunk's level 0 enters the
+double-float sum over chunks exactly and the levels below it, 2^-8 smaller,
+with FP32 roundings (2^-30 |L_c' Q_c|).  Integer-valued inputs split without
 truncation, so those products must come out exact: that checks that the
 tensor cores' FP32 accumulation of the digit products is exact."""
 import numpy as np
@@ -114,11 +116,13 @@ def _gram(ctx, L, Qs, ldt=S.FLOAT64):
 def _bound_gram(L, R):
     n = L.shape[0]
     b = np.zeros((L.shape[1], R.shape[1]))
+    c = np.zeros_like(b)
     for r0 in range(0, n, 64):
         ml = np.abs(L[r0:r0 + 64]).max(axis=0)
         mr = np.abs(R[r0:r0 + 64]).max(axis=0)
         b += 64.0 * np.outer(ml, mr)
-    return 2.0 ** -26 * b + 2.0 ** -50 * (np.abs(L).T @ np.abs(R))
+        c += np.abs(L[r0:r0 + 64].T @ R[r0:r0 + 64])
+    return 2.0 ** -29 * b + 2.0 ** -30 * c + 2.0 ** -50 * (np.abs(L).T @ np.abs(R))
 
 
 @pytest.mark.parametrize("n,h,widths", [(64, 1, []), (1000, 8, [(8, "f32")]),
