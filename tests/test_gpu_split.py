@@ -89,6 +89,26 @@ def test_split_update_wide_range_and_zeros(ctx):
     assert np.array_equal(Y[::97], Z[::97])
 
 
+def test_split_update_fp32_z_wide_range(ctx):
+    """An FP32 Z joins the product's exact integer in its units: Z far below
+    the product (rounded at half a unit), comparable to it, far above it (the
+    FP64 fallback), on zero rows of X and on a zero column of C."""
+    rng = np.random.default_rng(13)
+    n, h, w = 30000, 64, 40
+    X = rng.standard_normal((n, h)) * 10.0 ** rng.uniform(-8, 8, size=(n, 1))
+    X[::101] = 0.0
+    C = rng.standard_normal((h, w))
+    C[:, 3] = 0.0
+    Z = rng.standard_normal((n, w)) * 10.0 ** rng.uniform(-30, 30, size=(n, 1))
+    Z = Z.astype(np.float32).astype(np.float64)
+    Y = _update(ctx, X, C, Z, S.FLOAT32)
+    ref, b = _bound_update(X, C, Z)
+    err = np.abs(Y - ref)
+    assert np.all(err <= b), (err / b).max()
+    assert np.array_equal(Y[::101], Z[::101])
+    assert np.array_equal(Y[:, 3], Z[:, 3])
+
+
 def test_split_update_exact_on_integers(ctx):
     """Small integers split without truncation: the result must be exact."""
     rng = np.random.default_rng(5)
