@@ -680,14 +680,16 @@ __global__ void split_pencil_kernel(const double* __restrict__ Hx, const double*
   const int a = e % m, b = e / m;
   double g, h;
   if (a < k || b < k) {
+    // Gt = RS' [RS S] (k x (k + m), leading dimension k): S_c' RS_i at
+    // Gt[i + (k + c) k]
     if (a < k && b < k) {
       const double h1 = Hx[a + (size_t)b * k], h2 = Hx[b + (size_t)a * k];
       h = 0.5 * (h1 + h2);
-      g = 0.5 * ((lam[a] * h1 - Gt[b + (size_t)a * ld]) + (lam[b] * h2 - Gt[a + (size_t)b * ld]));
+      g = 0.5 * ((lam[a] * h1 - Gt[a + (size_t)(k + b) * k]) + (lam[b] * h2 - Gt[b + (size_t)(k + a) * k]));
     } else {
       const int i = a < k ? a : b, c = a < k ? b : a;
       h = Hx[i + (size_t)c * k];
-      g = lam[i] * h - Gt[c + (size_t)i * ld];
+      g = lam[i] * h - Gt[i + (size_t)(k + c) * k];
     }
   } else {
     const int ra = a - k, rb = b - k;  // offsets in [R P]

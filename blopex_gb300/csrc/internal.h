@@ -160,7 +160,8 @@ int gb_deflate_pencil(gpu_Context* ctx, double* G, double* H, int ld, int mtot, 
                       const int* dropped, int kx);
 /* the explicit pencil (G, H; m x m, m = k + nR + nP, leading dimension ld)
    of the split mode from Hx = X'[X R P] (ld k), Hr = R'[R P AR AP] (ld nR),
-   Hp = P'[P AP] (ld nP), Gt(c, i) = S_c' RS_i (ld ld; RS = lambda X - A X) and
+   Hp = P'[P AP] (ld nP), Gt = RS'[RS S] (ld k: S_c' RS_i at Gt[i + (k + c) k];
+   RS = lambda X - A X) and
    lambda: the X rows of G in residual form, lambda_i X_i'S_c - RS_i'S_c */
 int gb_split_pencil(gpu_Context* ctx, const double* Hx, const double* Hr, const double* Hp,
                     const double* Gt, double* G, double* H, int ld, const double* lam, int k,

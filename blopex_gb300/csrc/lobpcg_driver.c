@@ -921,19 +921,15 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
           if (gb_oz_gram(s->ctx, s->n, &cl, nP, F32, 1, cq, qw, qdt, Hp, nP)) return -2;
         }
         {
-          /* S' RS: small (it scales with the residual), so the TF32
-             tensor-core product carries enough accuracy; its H output is not
-             used (the exact one above is) */
-          blk_cols cx, cr, cp, cax, car, cap;
-          cols_idx(X, NULL, k, &cx, 0);
-          cols_idx(R, NULL, nR, &cr, 0);
-          cols_idx(P, act, nP, &cp, 0);
-          cols_idx(eb->RS, NULL, k, &cax, 0);
-          cols_idx(AR, NULL, nR, &car, 0);
-          cols_idx(AP, act, nP, &cap, 0);
-          if (gb_tc_gram(s->ctx, s->n, &cx, k, &cr, nR, &cp, nP, &cax, &car, &cap, 1, eb->tmp,
-                         eb->H2, k3))
-            return -2;
+          /* RS' [RS X R P] (RS and X's FP32 shadow): the residual-form X rows
+             need S' RS; exact for the stored FP32 values like the other
+             Grams (the first k columns, RS' RS, are not used) */
+          cols_idx(eb->RS, NULL, k, &cl, 0);
+          nq = 0;
+          cols_idx(X, NULL, k, &cq[nq], 0), qw[nq] = k, qdt[nq++] = F32;
+          cols_idx(R, NULL, nR, &cq[nq], 0), qw[nq] = nR, qdt[nq++] = F32;
+          if (nP) cols_idx(P, act, nP, &cq[nq], 0), qw[nq] = nP, qdt[nq++] = F32;
+          if (gb_oz_gram(s->ctx, s->n, &cl, k, F32, nq, cq, qw, qdt, eb->tmp, k)) return -2;
         }
         if (gb_split_pencil(s->ctx, Hx, Hr, Hp, eb->tmp, eb->G, eb->H, k3, s->lam, k, nR, nP))
           return -2;

@@ -444,20 +444,30 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
     prm.cols.col[c] = L->col[c];
     if ((uintptr_t)L->col[c] & 15) return gb_fail(ctx, "oz_gram: column %d of L not 16-byte aligned", c);
   }
-  int wtot = h;
+  // consecutive Q blocks of one dtype that fit 64 columns together share a
+  // tile (a solve's R and P blocks narrow as columns converge): the output
+  // columns keep their order, and every entry's digits and level sums are
+  // those of its own column pair, so only the work shrinks
+  int wtot = h, mq = 0;
   ozg_offsets qoff;
   for (int q = 0; q < nq; q++) {
     if (qw[q] < 0 || qw[q] > 64) return gb_fail(ctx, "oz_gram: block %d has %d columns", q, qw[q]);
-    prm.qw[q] = qw[q];
-    prm.qdt[q] = qdt[q];
-    qoff.q[q] = wtot;
-    for (int j = 0; j < qw[q]; j++) {
-      prm.cols.col[64 + 64 * q + j] = Q[q].col[j];
+    for (int j = 0; j < qw[q]; j++)
       if ((uintptr_t)Q[q].col[j] & 15)
         return gb_fail(ctx, "oz_gram: column %d of block %d not 16-byte aligned", j, q);
+    if (qw[q] == 0) continue;
+    if (mq == 0 || prm.qdt[mq - 1] != qdt[q] || prm.qw[mq - 1] + qw[q] > 64) {
+      prm.qw[mq] = 0;
+      prm.qdt[mq] = qdt[q];
+      qoff.q[mq] = wtot;
+      mq++;
     }
+    for (int j = 0; j < qw[q]; j++) prm.cols.col[64 + 64 * (mq - 1) + prm.qw[mq - 1] + j] = Q[q].col[j];
+    prm.qw[mq - 1] += qw[q];
     wtot += qw[q];
   }
+  nq = mq;
+  prm.nq = nq;
   qoff.q[nq] = wtot;
   const int ntiles = nq > 0 ? nq : 1;
   const long nchunks = (n + OZG_ROWS - 1) / OZG_ROWS;
@@ -484,7 +494,7 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
   oz_gram_reduce_kernel<<<(h * wtot + 255) / 256, 256, 0, (cudaStream_t)ctx->stream>>>(
       prm.partial, (int)gx, h, nq, qoff, wtot, G, ldg, prm.err, ctx->dcount + 5);
   double bytes = (ldt == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * h;
-  for (int q = 0; q < nq; q++) bytes += (qdt[q] == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * qw[q];
+  for (int q = 0; q < nq; q++) bytes += (prm.qdt[q] == GPU_MV_FLOAT64 ? 8.0 : 4.0) * n * prm.qw[q];
   gb_prof_end(ctx, &pr, bytes, 2.0 * n * h * wtot);
   gb_count_launch(2);
   return gb_cuda_check(ctx, (int)cudaGetLastError(), "oz_gram_reduce");

@@ -148,7 +148,11 @@ def _bound_gram(L, R):
 @pytest.mark.parametrize("n,h,widths", [(64, 1, []), (1000, 8, [(8, "f32")]),
                                         (100003, 64, [(64, "f32"), (64, "f32")]),
                                         (262144, 32, [(17, "f64"), (64, "f32")]),
-                                        (4099, 64, [(1, "f32"), (3, "f64"), (64, "f32")])])
+                                        (4099, 64, [(1, "f32"), (3, "f64"), (64, "f32")]),
+                                        # narrow blocks of one dtype share tiles
+                                        (50000, 16, [(8, "f32"), (8, "f32"), (20, "f32"), (30, "f32")]),
+                                        (20000, 8, [(5, "f32"), (7, "f32"), (9, "f32"), (11, "f32")]),
+                                        (7000, 5, [(3, "f64"), (2, "f64"), (4, "f32")])])
 def test_split_gram_matches_fp64(ctx, n, h, widths):
     rng = np.random.default_rng(n + h)
     L = rng.standard_normal((n, h)) * np.exp(rng.standard_normal((1, h)))
