@@ -792,6 +792,27 @@ static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
       s->mask[i] = s->h_norm[i] > fabs(s->h_lam[i]) * s->tol.relative + s->tol.absolute + DBL_EPSILON;
       if (s->mask[i]) act[nR++] = i;
     }
+    if (nR < 1 && split && refresh != 0) {
+      /* converged on the updated A X: confirm on the exact one before the
+         FP64 phase's check (the updated A X can understate a residual near
+         the tolerance by its FP32 terms, and an FP64 iteration costs several
+         split ones) */
+      refresh = 0;
+      gb_mv_set_mask_host(X64, NULL);
+      gb_mv_set_mask_host(AX64, NULL);
+      if (d_apply(s, s->A, s->Adata, X64, AX64)) return -2;
+      blk_cols x0, x1;
+      cols_idx(X64, NULL, k, &x0, 0);
+      cols_idx(AX64, NULL, k, &x1, 0);
+      if (gb_rayleigh_quotients(s->ctx, GPU_MV_FLOAT64, s->n, &x0, &x1, k, eb->rq, s->lam) ||
+          fetch_lambda(s) || split_residual(s, eb, X64, AX64, NULL, k))
+        return -2;
+      rs_stale = 0;
+      for (int i = 0; i < k; i++) {
+        s->mask[i] = s->h_norm[i] > fabs(s->h_lam[i]) * s->tol.relative + s->tol.absolute + DBL_EPSILON;
+        if (s->mask[i]) act[nR++] = i;
+      }
+    }
     if (nR < 1) break;
     nP = haveP ? nR : 0; /* P restricted to the active columns */
     {
