@@ -49,3 +49,19 @@ def test_traffic_entries_are_filtered_by_workload(tmp_path, monkeypatch):
 def test_committed_traffic_file_names_its_workloads():
     traffic = bench.load_traffic("c2")
     assert "gram" in traffic and traffic["gram"]["bytes_per_launch"] > 0
+
+
+def test_nested_rayleigh_ritz_stages_stay_out_of_the_total():
+    # sygv's record spans its rr_* stages and the fallback gate: counting
+    # them again would inflate the total the shares are taken of
+    kt = {"oz_gram": _v(30.0, 0, 0), "sygv": _v(10.0, 0, 0), "rr_tridiag": _v(4.0, 0, 0),
+          "rr_bisect": _v(3.0, 0, 0), "sygv_fp64_gate": _v(0.1, 0, 0), "blas1": _v(60.0, 0, 0)}
+    assert bench.nested("rr_tridiag") and bench.nested("sygv_fp64_gate")
+    assert not bench.nested("sygv") and not bench.nested("blas1")
+    assert bench.top_level_ms(kt) == 100.0
+    assert bench.top_level_ms({}) == 1.0
+
+
+def test_reference_arm_scales_by_the_recorded_fp64_iteration_count():
+    assert bench.CONFIGS["c3m"]["fp64_iterations"] == 176
+    assert bench.CONFIGS["c3"]["fp64_iterations"] == 565
