@@ -786,6 +786,14 @@ def main():
                                     fp64_arith=args.mode == "fp64", tf32_peak=tf32_peak)
                  for nm in ("tc_gram", "tc_xc_update", "oz_xc_update", "oz_gram",
                             "stencil7_fp32", "spmm_csr_fp32") if nm in ktimes}
+    # the split-operand products are FP64-accurate products bound by their
+    # digit work: their rate beside the FP64 pipe they replace
+    for nm in ("oz_xc_update", "oz_gram"):
+        if nm in rooflines:
+            v = ktimes[nm]
+            eq = v["flops"] / (v["ms"] / 1e3) / 1e12
+            rooflines[nm]["fp64_accurate_tflops"] = eq
+            rooflines[nm]["over_fp64_pipe"] = eq / fp64_peak
 
     line = {"metric": metric_name(cfg, res, args.mode), "value": secs, "unit": "s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
