@@ -1,14 +1,20 @@
 #!/usr/bin/env python
 """Benchmark of the LOBPCG hot path on GB300 (one JSON line on stdout).
 
-Workload (default, --config c2): the "plain FP64 on GPU" case -- 3D 7-point
-Dirichlet Laplacian 128^3 (n = 2,097,152, CSR int32 / FP64, nnz =
-14,581,760), block size k = 32, Jacobi preconditioner, X0 = 2*drand48()-1
-from seed 1, tolerance 1e-8, at most 300 iterations.  One step = one full
-lobpcg_solve_double call from X0 to exit (converged or maxit).  Synthetic
-data generated by the seeded builders in blopex_gb300/problems.py.
+Workload (default, --config c3m): time to k eigenpairs at residual 1e-8 of
+the matrix-free variable-coefficient 7-point stencil (faces exp(N(0,1)),
+seed 2), k = 64, X0 = 2*drand48()-1 from seed 2, preconditioner 20
+Jacobi-CG steps on A, in mixed precision with the plain FP64 GPU path
+beside: timed as whole solves at 128^3 (n = 2,097,152), and the 256^3 case
+(n = 16,777,216) solved once per arm beside it (`full_size`), each with its
+eigenvalue error and largest subspace angle against the FP64 arm.  One
+step = one full lobpcg_solve_double call from X0 to exit.  Synthetic data
+from the seeded builders in blopex_gb300/problems.py.  Other workloads:
+--config c2 (CSR Laplacian 128^3, k = 32, Jacobi, maxit 300), c4 (2D
+diffusion forward + gradient), c5 (generalized 27-point 100^3, k = 128,
+forward + gradient), c1 (20^3).
 
-value  = seconds per solve with X0, the matrix and the preconditioner
+value  = seconds per solve with X0, the operator and the preconditioner
          resident in HBM (max over ranks), CUDA events on the solver stream;
 e2e    = the same through the C ABI with X0 uploaded from pinned host memory
          and the Ritz vectors + eigenvalues read back, every step;
@@ -19,9 +25,9 @@ cpu_baseline = the C restatement of the reference (oracle/, scalar loops,
          one core) on a bounded sample, scaled to the full workload.
 
 --impl reference times that CPU implementation alone (the reference's own
-algorithm on the host cores; the compiled reference itself is not available
-on the GPU host).  Under torchrun each rank runs an independent replica
-(the solver does not shard: replicas only).
+algorithm on one host core, its LAPACK calls single-threaded; the compiled
+reference itself is not available on the GPU host).  Under torchrun each
+rank runs an independent replica (the solver does not shard: replicas only).
 """
 from __future__ import annotations
 
@@ -33,6 +39,11 @@ import subprocess
 import sys
 import tempfile
 import time
+
+if "--impl" in sys.argv and "reference" in sys.argv:
+    # the reference is single-threaded: its LAPACK calls too (set before the
+    # BLAS library loads)
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 import numpy as np
 
@@ -536,13 +547,17 @@ def run_reference(args, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    try:  # one core, as the reference runs
+        os.sched_setaffinity(0, {min(os.sched_getaffinity(0))})
+    except (AttributeError, OSError):
+        pass
     for _ in range(args.warmup):
         cpu_baseline(cfg, sample_grid=24)
     vals = [cpu_baseline(cfg, sample_grid=24) for _ in range(args.steps)]  # each a bounded sample
     v = statistics.median(x["value"] for x in vals)
     cb = dict(vals[0])
     cb["value"] = v
-    line = {"impl": "reference", "metric": metric_name(cfg, None, "fp64"), "value": v, "unit": "s",
+    line = {"impl": "reference", "metric": metric_name(cfg, None, args.mode), "value": v, "unit": "s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
