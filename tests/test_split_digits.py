@@ -15,6 +15,9 @@ values just below a power of two, both signs, values many binades below E
     are zero);
   * the digits rebuild the 32-bit fixed point value to within 1/2 unit;
   * the level sums over 64 rows of the worst digits stay below 2^24.
+The same for the block update (oz_xc.cu): six 7-bit digits per value of X
+(three exact 14-bit parts) and of C (balanced by a bias), rebuilding the
+42-bit fixed point exactly, and level sums over 64 terms below 2^22.
 """
 import numpy as np
 import pytest
@@ -130,3 +133,56 @@ def test_level_sums_below_2_24_over_a_chunk():
     for L in range(4):
         worst = 64 * sum(dmax[t] * dmax[L - t] for t in range(L + 1))
         assert worst < 2 ** 24, (L, worst)
+
+
+# ------------------------------------------------ the update's six 7-bit digits
+def update_x_digits(v, E):
+    """ozx_digits (oz_xc.cu): the 42-bit fixed point in three 14-bit parts,
+    each cut into a rounded 7-bit digit and its remainder."""
+    U = fixed64(v, E, F=42)
+    s = -1.0 if v < 0 else 1.0
+    parts = [U >> 28, (U >> 14) & 0x3FFF, U & 0x3FFF]
+    d = []
+    for p in parts:
+        c = s * float(p)
+        a = rint32(c * 2.0 ** -7)
+        d += [a, np.float64(f32(c - 128.0 * a))]
+    return U, d
+
+
+def update_c_digits(U, neg, S=6):
+    """oz_digits<S> (oz_common.cuh): balanced 7-bit digits by a bias of 64
+    on every digit below the top one."""
+    bias = sum(64 << (7 * (S - 1 - t)) for t in range(1, S))
+    V = U + bias
+    d = [V >> (7 * (S - 1))] + [((V >> (7 * (S - 1 - t))) & 127) - 64 for t in range(1, S)]
+    return [-x if neg else x for x in d]
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_update_digits_exact_and_bounded(seed):
+    rng = np.random.default_rng(seed)
+    vals = _adversarial(rng, 150)
+    E = max(bexp64(x) for x in vals)
+    for v in vals:
+        U, d = update_x_digits(v, E)
+        assert all(float(x).is_integer() for x in d)
+        assert all(abs(x) <= 128 for x in d[0::2]) and all(abs(x) <= 64 for x in d[1::2])
+        assert all(_is_bf16_exact(x) for x in d)
+        rebuilt = sum(d[t] * 2.0 ** (7 * (5 - t)) for t in range(6))
+        assert rebuilt == (-U if v < 0 else U)
+        dc = update_c_digits(U, v < 0)
+        assert abs(dc[0]) <= 129 and all(abs(x) <= 64 for x in dc[1:])
+        assert sum(dc[t] * 2 ** (7 * (5 - t)) for t in range(6)) == (-U if v < 0 else U)
+
+
+def test_update_level_sums_below_2_22_over_64_columns():
+    """h <= 64 contraction terms per output: every kept level L = t + u < 6
+    of the update's digit products (X: |d| <= 128 / 64 alternating; C: top
+    digit <= 129, the rest <= 64) sums below 2^22, so two levels combine in a
+    32-bit integer (S_L 128 + S_{L+1}) as the epilogue does."""
+    dx = [128, 64, 128, 64, 128, 64]
+    dc = [129, 64, 64, 64, 64, 64]
+    for L in range(6):
+        worst = 64 * sum(dx[t] * dc[L - t] for t in range(L + 1))
+        assert worst < 2 ** 22, (L, worst)
