@@ -253,10 +253,9 @@ def cpu_baseline(cfg, iterations=None, sample_grid=32):
     multiplied by the iteration count of the FP64 GPU path on the workload
     (the same algorithm: iteration counts agree within 2 where parity is
     pinned), or by the configuration's recorded count.  Extrapolated: a full
-    CPU solve of the 256^3 case would take days.  The oracle's operators
-    cover the Jacobi preconditioner only; an inner-CG preconditioner would
-    add its operator applications (~15 % of the reference's per-iteration
-    work at k = 64), so the figure is a lower bound for that case."""
+    CPU solve of the 256^3 case would take days.  The preconditioner is the
+    configuration's: Jacobi, or the inner CG (HYPRE's -pcgitr) on the
+    sample's operator with Jacobi inside."""
     from blopex_gb300 import problems as P
     from oracle import oracle as O
     O.build(ref=False)
@@ -267,6 +266,9 @@ def cpu_baseline(cfg, iterations=None, sample_grid=32):
     csr = op[1] if op[0] == "csr" else P.stencil7_to_csr(*op[1])
     A = O.csr(*csr)
     T = O.diag(tdiag)
+    precond = cfg.get("precond", "")
+    if precond.startswith("pcg"):
+        T = O.pcg(A, T, int(precond[3:]))
     t0 = time.perf_counter()
     O.solve(A, x0, T=T, atol=cfg["tol"], maxit=1, history=False)
     t1 = time.perf_counter()
@@ -279,7 +281,9 @@ def cpu_baseline(cfg, iterations=None, sample_grid=32):
     value = (setup + its * per_it) * scale
     return {"value": value, "unit": "s", "cores": 1, "host_cores": os.cpu_count(),
             "kind": "port",
-            "sample": f"oracle C restatement, {s}^3 grid k={cfg['k']} Jacobi, 1 and 3 iterations "
+            "sample": f"oracle C restatement, {s}^3 grid k={cfg['k']} "
+                      f"{'inner CG ' + precond[3:] + ' steps' if precond.startswith('pcg') else 'Jacobi'}, "
+                      f"1 and 3 iterations "
                       f"({t2 - t0:.1f} s measured), per-iteration {per_it:.3f} s scaled by n "
                       f"x{scale:.0f} and to {its} iterations (extrapolated)",
             "per_iteration_s_full_n": per_it * scale, "iterations_assumed": its}

@@ -33,7 +33,7 @@ typedef void (*dpotrf_fn)(char*, int*, double*, int*, int*);
 /* ------------------------------------------------------------------ */
 
 enum { OP_NONE = 0, OP_CSR = 1, OP_DENSE = 2, OP_DIAG = 3, OP_STENCIL7 = 4,
-       OP_STENCIL5 = 5, OP_STENCIL27 = 6 };
+       OP_STENCIL5 = 5, OP_STENCIL27 = 6, OP_PCG = 7 };
 
 typedef struct {
   int n;
@@ -85,10 +85,76 @@ typedef struct {
   const void* data;
 } oracle_op;
 
+/* T ~ inv(A): `iters` steps of conjugate gradients on A y = x from y = 0,
+   preconditioned by M (kind OP_NONE: none).  The inner preconditioner of
+   HYPRE's LOBPCG driver with -pcgitr (blopex_hypre/krylov/HYPRE_lobpcg.c:
+   317-320, a fixed number of PCG steps per application), one column at a
+   time; a coefficient with a zero numerator or denominator is 0. */
+typedef struct {
+  oracle_op A;
+  oracle_op M;
+  int iters;
+} oracle_pcg;
+
+static void op_apply_col(const oracle_op* op, long n, const double* x, double* y);
+
+static void pcg_apply_col(const oracle_pcg* T, long n, const double* x, double* y)
+{
+  double* w = (double*)calloc(4 * (size_t)n, sizeof(double));
+  double *r, *z, *p, *q;
+  double rho = 0.0, rho2, pq, alpha, beta;
+  long i;
+  int it;
+  if (!w) {
+    for (i = 0; i < n; i++) y[i] = 0.0;
+    return;
+  }
+  r = w;
+  z = w + n;
+  p = w + 2 * n;
+  q = w + 3 * n;
+  for (i = 0; i < n; i++) {
+    y[i] = 0.0;
+    r[i] = x[i];
+  }
+  if (T->M.kind != OP_NONE)
+    op_apply_col(&T->M, n, r, z);
+  else
+    for (i = 0; i < n; i++) z[i] = r[i];
+  for (i = 0; i < n; i++) {
+    p[i] = z[i];
+    rho += r[i] * z[i];
+  }
+  for (it = 0; it < T->iters; it++) {
+    op_apply_col(&T->A, n, p, q);
+    pq = 0.0;
+    for (i = 0; i < n; i++) pq += p[i] * q[i];
+    alpha = (pq != 0.0 && rho != 0.0) ? rho / pq : 0.0;
+    for (i = 0; i < n; i++) {
+      y[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+    }
+    if (it + 1 == T->iters) break;
+    if (T->M.kind != OP_NONE)
+      op_apply_col(&T->M, n, r, z);
+    else
+      for (i = 0; i < n; i++) z[i] = r[i];
+    rho2 = 0.0;
+    for (i = 0; i < n; i++) rho2 += r[i] * z[i];
+    beta = (rho != 0.0 && rho2 != 0.0) ? rho2 / rho : 0.0;
+    for (i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+    rho = rho2;
+  }
+  free(w);
+}
+
 static void op_apply_col(const oracle_op* op, long n, const double* x, double* y)
 {
   long r;
   switch (op->kind) {
+  case OP_PCG:
+    pcg_apply_col((const oracle_pcg*)op->data, n, x, y);
+    break;
   case OP_CSR: {
     const oracle_csr* A = (const oracle_csr*)op->data;
     int p;

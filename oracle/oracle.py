@@ -29,7 +29,7 @@ REF_SO = os.path.join(HERE, "_ref", "libblopex_ref.so")
 # the reference checkout, when this machine has one (no default location)
 REF_SRC = os.environ.get("BLOPEX_REFERENCE_DIR", "")
 
-OP_NONE, OP_CSR, OP_DENSE, OP_DIAG, OP_STENCIL7, OP_STENCIL5, OP_STENCIL27 = range(7)
+OP_NONE, OP_CSR, OP_DENSE, OP_DIAG, OP_STENCIL7, OP_STENCIL5, OP_STENCIL27, OP_PCG = range(8)
 
 
 def build(ref: bool = True) -> None:
@@ -91,6 +91,10 @@ class _ST5(ctypes.Structure):
 class _ST27(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("w", ctypes.c_void_p), ("shift", ctypes.c_double)]
+
+
+class _PCG(ctypes.Structure):
+    _fields_ = [("A", _OpC), ("M", _OpC), ("iters", ctypes.c_int)]
 
 
 def _p(a: np.ndarray) -> int:
@@ -179,6 +183,14 @@ def lib():
 
 def _opc(op: Operator) -> _OpC:
     return _OpC(op.kind, _opc_ptr(op))
+
+
+def pcg(A: Operator, M: Operator, iters: int) -> Operator:
+    """T ~ inv(A) by `iters` steps of CG on A preconditioned by M (NONE: none),
+    the inner preconditioner of HYPRE's LOBPCG driver with -pcgitr
+    (blopex_hypre/krylov/HYPRE_lobpcg.c:317-320)."""
+    s = _PCG(_opc(A), _opc(M), iters)
+    return Operator(OP_PCG, s, (A, M))
 
 
 @dataclass

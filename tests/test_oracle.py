@@ -123,3 +123,49 @@ def test_stencil_operators_match_csr():
     cz = np.zeros((2, 6, 10))
     y2 = O.apply(O.stencil7(10, 6, 1, sx[None], sy[None], cz), x)
     np.testing.assert_allclose(y1, y2, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("jacobi", [True, False])
+def test_pcg_preconditioner_recurrence(jacobi):
+    """The oracle's inner-CG preconditioner (HYPRE -pcgitr semantics) against
+    the same recurrence in numpy, column by column, and T r = A^-1 r once the
+    steps exceed n (CG on an SPD matrix is exact in n steps, up to rounding)."""
+    cx, cy, cz = P.stencil7_coefficients(5, 4, 3, seed=8)
+    rp, ci, va = P.stencil7_to_csr(cx, cy, cz)
+    n = 60
+    A = np.zeros((n, n))
+    for r in range(n):
+        A[r, ci[rp[r]:rp[r + 1]]] = va[rp[r]:rp[r + 1]]
+    M = 1.0 / np.diag(A)
+    x = np.random.default_rng(4).standard_normal((n, 3))
+
+    def ref(steps):
+        out = np.zeros_like(x)
+        for j in range(x.shape[1]):
+            r = x[:, j].copy()
+            z = M * r if jacobi else r.copy()
+            p = z.copy()
+            rho = r @ z
+            y = np.zeros(n)
+            for it in range(steps):
+                q = A @ p
+                pq = p @ q
+                alpha = rho / pq if (pq != 0 and rho != 0) else 0.0
+                y += alpha * p
+                r -= alpha * q
+                if it + 1 == steps:
+                    break
+                z = M * r if jacobi else r
+                rho2 = r @ z
+                beta = rho2 / rho if (rho != 0 and rho2 != 0) else 0.0
+                p = z + beta * p
+                rho = rho2
+            out[:, j] = y
+        return out
+
+    Mop = O.diag(M) if jacobi else O.NONE
+    for steps in (1, 5, 12):
+        T = O.pcg(O.csr(rp, ci, va), Mop, steps)
+        np.testing.assert_allclose(O.apply(T, x), ref(steps), rtol=1e-12, atol=1e-14)
+    T = O.pcg(O.csr(rp, ci, va), Mop, 2 * n)
+    np.testing.assert_allclose(O.apply(T, x), np.linalg.solve(A, x), rtol=1e-8)
