@@ -244,3 +244,38 @@ def test_mixed_phase_options(ctx, opts):
     tol = np.abs(r.lam) * case.rtol + case.atol + np.finfo(float).eps
     assert np.all(r.res <= tol)
     np.testing.assert_allclose(r.lam, g["lambda"], rtol=max(LAMBDA_RTOL, 3 * _spread(g)))
+
+
+def test_generalized_k128_mixed_against_eigsh(ctx):
+    """The generalized 27-point configuration's shape at 24^3 (k = 128 > 64,
+    B = lumped mass: the mixed mode's FP32 phase on the CUDA-core kernels,
+    then the FP64 loop): converged to 1e-8, with true residuals
+    ||A x - lambda B x|| from fresh operator applications below it, and the
+    eigenvalues of scipy's shift-invert Lanczos to 1e-10."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    g, k = 24, 128
+    n = g ** 3
+    w = P.stencil27_weights(g, g, g, seed=4)
+    b = P.mass_diagonal(n, seed=14)
+    rp, ci, va = P.stencil27_to_csr(g, g, g, w, 0.5)
+    Acsr = sp.csr_matrix((va, ci, rp), shape=(n, n))
+    ref = np.sort(sla.eigsh(Acsr, k=k + 4, M=sp.diags(b), sigma=0, which="LM",
+                            return_eigenvectors=False))[:k]
+    A = S.Stencil27(ctx, g, g, g, w, 0.5)
+    B = S.Diagonal(ctx, b)
+    T = S.PCGPreconditioner(ctx, A, S.Diagonal(ctx, 1.0 / Acsr.diagonal()), 20)
+    X = S.MultiVector(ctx, n, k)
+    X.set_random(4)
+    ctx.set_options(precision=S.MIXED)
+    try:
+        r = S.lobpcg_solve_double(X, A, B=B, T=T, atol=1e-8, rtol=1e-50, maxit=1000, history=False)
+    finally:
+        ctx.set_options(precision=S.FP64)
+    assert r.flag == 0, (r.iterations, ctx.last_error())
+    AX, BX = S.MultiVector(ctx, n, k), S.MultiVector(ctx, n, k)
+    A.apply(X, AX)
+    B.apply(X, BX)
+    true_res = np.linalg.norm(AX.to_host() - BX.to_host() * r.lam[None, :], axis=0)
+    assert true_res.max() <= 1e-8, true_res.max()
+    np.testing.assert_allclose(r.lam, ref, rtol=1e-10)
