@@ -703,15 +703,21 @@ static int split_residual(solver_t* s, explicit_bufs* eb, gpu_MultiVector* X64,
 }
 
 /*
- * The FP32 phase of the mixed mode: block LOBPCG with explicit Gram
- * matrices.  Each iteration forms G = [X R P]'[AX AR AP] and
- * H = [X R P]'[BX BR BP] in one pass each (no separate orthonormalisation
- * passes over R and P), solves the scaled FP64 pencil
- * (D G D) c = theta (D H D) c on the device -- dropping P when the pencil is
- * not definite (the restart of lobpcg.c:1056-1063 done on the small side) --
- * and updates P = [R P] C_RP, X = X C_X + P (and their A / B images) with
- * one combined kernel each.  Returns 0 (converged, maxit, or handed over to
- * FP64 with ctl->handed_over set) or -2 on a CUDA error.
+ * The explicit phase of the mixed mode: block LOBPCG with explicit Gram
+ * matrices.  Each iteration forms the pencil G = [X R P]'[AX AR AP],
+ * H = [X R P]'[BX BR BP] (no separate orthonormalisation passes over R and
+ * P), orthonormalises it on the small side and solves it in FP64 on the
+ * device -- dropping P when its block is not definite (the restart of
+ * lobpcg.c:1056-1063 done on the small side) -- and updates
+ * P = [R P] C_RP, X = X C_X + P and their images.  Two variants:
+ *   split (B = I, no constraints, k <= 64, the tensor-core kernels usable):
+ *     X and A X carried in FP64, the pencil from FP64-accurate split-operand
+ *     Grams (oz_gram.cu; the X rows in residual form), X and A X updated by
+ *     the split-operand block update (oz_xc.cu); iterates to the tolerance;
+ *   FP32: FP32 blocks, TF32 / compensated tensor-core or CUDA-core
+ *     products; hands over to the FP64 iteration at its floor.
+ * Returns 0 (converged, maxit, or handed over to FP64 with
+ * ctl->handed_over set) or -2 on a CUDA error.
  */
 static int phase_explicit(solver_t* s, phase_ctl* ctl, explicit_bufs* eb)
 {
