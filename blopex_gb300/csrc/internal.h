@@ -232,6 +232,11 @@ int gb_scale_rows(gpu_Context* ctx, double* C, const double* d, int ld, int m, i
 /* ---------------- operators (operators.cu) ---------------- */
 struct gpu_Operator;
 int gb_operator_apply(struct gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
+/* Y = A X with dot_out[c] = X_c' Y_c (device, one per active column) folded
+   into the operator's kernel: 0, or 1 when the operator cannot (nothing was
+   done), -1 on an error */
+int gb_operator_apply_dot(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y,
+                          double* dot_out);
 
 #ifdef __cplusplus
 }

@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
     int nx, int ny, int nz, const float* __restrict__ cx, const float* __restrict__ cy,
     const float* __restrict__ cz, float shift, const __grid_constant__ CUtensorMap tm_c,
     const __grid_constant__ CUtensorMap tm_z, const __grid_constant__ st7t_cols XC,
-    const __grid_constant__ blk_cols Y, int w, int* err)
+    const __grid_constant__ blk_cols Y, int w, int* err, double* __restrict__ dotp)
 {
   __shared__ __align__(128) float ring[ST7T_DEPTH * ST7T_SLOT];
   __shared__ __align__(8) uint64_t bar[ST7T_DEPTH];
@@ -495,6 +495,7 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
       issued++;
     }
     float* y = (float*)Y.col[col] + cell0;
+    float xs = 0.f, xc = 0.f;  // this thread's share of x' (A x): compensated sum
     if (go) {
       const float* sl = ring + ST7T_SLOT * slot;
       float cv[6];
@@ -506,11 +507,32 @@ __global__ void __launch_bounds__(256) st7_tma_kernel(
         const float v1 = sl[m - 1], v2 = sl[m + 1];
         const float v5 = sl[ST7T_BELOW + (4 * ty + s) * 32 + tx];
         const float v6 = sl[ST7T_ABOVE + (4 * ty + s) * 32 + tx];
-        if (valid[s])
-          __stcs(y + (long)nx * s, dg[s] * cv[s + 1] - ww[s] * v1 - we[s] * v2 - ws[s] * cv[s] -
-                                       wn[s] * cv[s + 2] - wb[s] * v5 - wt[s] * v6);
+        if (valid[s]) {
+          const float yv = dg[s] * cv[s + 1] - ww[s] * v1 - we[s] * v2 - ws[s] * cv[s] -
+                           wn[s] * cv[s + 2] - wb[s] * v5 - wt[s] * v6;
+          __stcs(y + (long)nx * s, yv);
+          if (dotp) acc_prod32(xs, xc, cv[s + 1], yv);
+        }
       }
-    } else {
+    }
+    if (dotp) {
+      // per warp: exact products in compensated FP32 sums, combined across
+      // the lanes by two-sums, into FP64 partials that a second kernel sums
+      // in a fixed order (the inner CG's p' A p, as accurate as its
+      // separate inner-product kernel)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, xs, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, xc, o);
+        const float t2 = __fadd_rn(xs, s2);
+        const float bp = __fsub_rn(t2, xs);
+        const float e = __fadd_rn(__fsub_rn(xs, __fsub_rn(t2, bp)), __fsub_rn(s2, bp));
+        xs = t2;
+        xc = __fadd_rn(__fadd_rn(xc, c2), e);
+      }
+      if (tx == 0) dotp[(long)col * gridDim.x * 8 + blockIdx.x * 8 + ty] = go ? (double)xs + (double)xc : 0.0;
+    }
+    if (!go) {
 #pragma unroll
       for (int s = 0; s < 4; s++)
         if (valid[s]) y[(long)nx * s] = __int_as_float(0x7fc00000);  // NaN: output incomplete
@@ -869,9 +891,36 @@ static int st7t_maps(const gpu_Operator* op, const gpu_MultiVector* X, CUtensorM
 
 static int pcg_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y);
 
+// the per-column sums of the stencil kernel's warp partials, in a fixed order
+__global__ void __launch_bounds__(256) st7t_dot_reduce_kernel(const double* __restrict__ parts,
+                                                              long nparts, double* __restrict__ out)
+{
+  const double* p = parts + (size_t)blockIdx.x * nparts;
+  double acc = 0.0;
+  for (long i = threadIdx.x; i < nparts; i += blockDim.x) acc += p[i];
+  const double t = block_sum256(acc);
+  if (threadIdx.x == 0) out[blockIdx.x] = t;
+}
+
+static int operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y, double* dot_out);
+
 extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y)
 {
-  if (op->kind == OPK_PCG) return pcg_apply(op, X, Y);
+  return operator_apply(op, X, Y, NULL);
+}
+
+// Y = A X and out[c] = X_c' Y_c in one pass where the operator's kernel can
+// fold the inner products in (the FP32 TMA 7-point stencil): 0; 1 when it
+// cannot (nothing done: apply and take the inner products apart); -1 on error
+extern "C" int gb_operator_apply_dot(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y,
+                                     double* dot_out)
+{
+  return operator_apply(op, X, Y, dot_out);
+}
+
+static int operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_MultiVector* Y, double* dot_out)
+{
+  if (op->kind == OPK_PCG) return dot_out ? 1 : pcg_apply(op, X, Y);
   gpu_Context* ctx = op->ctx;
   if (X->size != op->n || Y->size != op->n)
     return gb_fail(ctx, "operator of size %ld applied to blocks of %ld / %ld rows", op->n,
@@ -893,6 +942,14 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
   // smooth block |A x| << |A| |x|, and FP32 products and sums would lose the
   // cancellation that A x consists of
   const int acc64 = f32 && ctx->op_accurate && (op->kind == OPK_CSR || op->kind == OPK_ST7);
+  // the FP32 7-point stencil staged by TMA (nx a multiple of 4, aligned block)
+  CUtensorMap tmc, tmz;
+  const int tma = op->kind == OPK_ST7 && f32 && !acc64 && st7t_maps(op, X, &tmc, &tmz) == 0;
+  if (dot_out && !tma) return 1;
+  const unsigned st7t_ctas = (unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz);
+  double* dparts = NULL;
+  if (dot_out && !(dparts = (double*)gb_workspace(ctx, sizeof(double) * 8 * (size_t)st7t_ctas * w)))
+    return -1;
   const long n = op->n;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   const double es = f32 ? 4.0 : 8.0;
@@ -946,21 +1003,24 @@ extern "C" int gb_operator_apply(gpu_Operator* op, gpu_MultiVector* X, gpu_Multi
                                                                op->vals, xc, yc, w);
       break;
     case OPK_ST7: {
-      CUtensorMap tmc, tmz;
       const unsigned tb = (unsigned)(((op->nx + ST_TX - 1) / ST_TX) * ((op->ny + ST_TY - 1) / ST_TY) *
                                      (long)op->nz);
       if (acc64)
         st7_kernel<float, double><<<tb, ST_TX * ST_TY, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c[0],
                                                                     op->c[1], op->c[2], op->shift,
                                                                     xc, yc, w);
-      else if (f32 && st7t_maps(op, X, &tmc, &tmz) == 0) {
+      else if (tma) {
         st7t_cols pc;
         for (int c = 0; c < w; c++) pc.c[c] = X->active[c];
         if (tc_apply_wait_polls(ctx->opt.wait_polls, S(ctx)) != cudaSuccess)
           return gb_fail(ctx, "stencil7: cannot set the wait limit");
-        st7_tma_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
-                         0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1], op->c32[2],
-                                      (float)op->shift, tmc, tmz, pc, yc, w, ctx->dcount + 5);
+        st7_tma_kernel<<<st7t_ctas, 256, 0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
+                                                      op->c32[2], (float)op->shift, tmc, tmz, pc, yc,
+                                                      w, ctx->dcount + 5, dparts);
+        if (dot_out) {
+          st7t_dot_reduce_kernel<<<w, 256, 0, S(ctx)>>>(dparts, 8L * st7t_ctas, dot_out);
+          gb_count_launch(1);
+        }
       } else if (f32 && st7_ring_ok(op, &xc, w))
         st7_ring_kernel<<<(unsigned)(((op->nx + 31) / 32) * ((op->ny + 31) / 32) * (long)op->nz), 256,
                           0, S(ctx)>>>(op->nx, op->ny, op->nz, op->c32[0], op->c32[1],
@@ -1501,8 +1561,12 @@ static int pcg32_fused(gpu_Operator* op, gpu_MultiVector* X, const blk_cols* cx,
   if (gb_dot_reduce(ctx, partial, (int)grid.x, w, rho, idx)) return -1;
   (void)X;
   for (int it = 0; it < op->iters; it++) {
-    if (gb_operator_apply(op->inner, p, q)) return -1;
-    if (gb_dot_cols(ctx, GPU_MV_FLOAT32, n, cp, cq, w, pq, idx)) return -1;
+    // q = A p with p' q folded into the operator's kernel where it can be
+    const int fused = gb_operator_apply_dot(op->inner, p, q, pq);
+    if (fused < 0) return -1;
+    if (fused == 1 && (gb_operator_apply(op->inner, p, q) ||
+                       gb_dot_cols(ctx, GPU_MV_FLOAT32, n, cp, cq, w, pq, idx)))
+      return -1;
     pcg_ratio_kernel<<<1, BLK_MAXCOLS, 0, S(ctx)>>>(w, rho, pq, al);
     gb_count_launch(1);
     const bool last = it + 1 == op->iters;
