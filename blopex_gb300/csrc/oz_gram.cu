@@ -100,7 +100,6 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ __align__(16) int part[1024];  // per (column, 8-row group) largest exponent
   // this tile's column pointers and kinds (0 absent, 1 FP32, 2 FP64) in shared
   // memory: a runtime index into the kernel-parameter table is slow
   __shared__ const void* s_col[128];
@@ -196,27 +195,46 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       const long r0 = (blockIdx.x + c * gridDim.x) * OZG_ROWS;
       const int rows = (int)min((long)OZG_ROWS, prm.n - r0);
       const unsigned char* raw = raws + slot * OZG_RAW;
-      // pass 1: largest exponent of each (column, 8-row group), the group's
-      // eight values read with 16-byte loads
+      // pass 1: each column's largest exponent over the chunk.  The eight
+      // 8-row groups of column j sit in eight consecutive lanes (every lane
+      // of a warp runs the same number of iterations), which combine theirs
+      // by shuffles.  Only the maximum matters here, so the lanes read their
+      // 16-byte pieces in rotated orders: the eight lanes of a column then
+      // touch eight different bank groups.
       for (int u = p; u < 1024; u += OZG_NPROD) {
         const int j = u >> 3, q = u & 7;
         const int kind = abort_flag ? 0 : s_kind[j];
         const int nr = min(8, rows - 8 * q);
         int e = 0;
         if (kind == 2) {
-          double v[8];
-          ozg_load8(raw + j * OZG_COLSTRIDE + 64 * q, v);
+          const unsigned char* src = raw + j * OZG_COLSTRIDE + 64 * q;
 #pragma unroll
-          for (int x = 0; x < 8; x++)
-            if (x < nr) e = max(e, oz_bexp64(v[x]));
+          for (int x = 0; x < 4; x++) {
+            const int xx = (x + (q >> 1)) & 3;  // rows 2 xx, 2 xx + 1
+            const double2 d = *(const double2*)(src + 16 * xx);
+            if (2 * xx < nr) e = max(e, oz_bexp64(d.x));
+            if (2 * xx + 1 < nr) e = max(e, oz_bexp64(d.y));
+          }
         } else if (kind == 1) {
-          float v[8];
-          ozg_load8(raw + j * OZG_COLSTRIDE + 32 * q, v);
+          const unsigned char* src = raw + j * OZG_COLSTRIDE + 32 * q;
 #pragma unroll
-          for (int x = 0; x < 8; x++)
-            if (x < nr) e = max(e, oz_bexp32(v[x]));
+          for (int x = 0; x < 2; x++) {
+            const int hx = x ^ ((q >> 2) & 1);  // rows 4 hx .. 4 hx + 3
+            const float4 f = *(const float4*)(src + 16 * hx);
+            if (4 * hx < nr) e = max(e, oz_bexp32(f.x));
+            if (4 * hx + 1 < nr) e = max(e, oz_bexp32(f.y));
+            if (4 * hx + 2 < nr) e = max(e, oz_bexp32(f.z));
+            if (4 * hx + 3 < nr) e = max(e, oz_bexp32(f.w));
+          }
         }
-        part[u] = e;
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, 4));
+        // the chunk scale (absent columns: 0).  Slot c mod 4 was last read by
+        // the epilogue of chunk c - 4, which finished before the MMAs of
+        // chunk c - 2 started (their accumulator buffer), and those completed
+        // before the previous chunk's pass 2 (its a_empty wait)
+        if (q == 0) cexp[c & 3][j] = e;
       }
       named_bar(1, OZG_NPROD);
       // the digit slices are free once the previous chunk's MMAs completed
@@ -226,11 +244,14 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       }
       if (!abort_flag) {
         tc_fence_after();
-        // pass 2: the digits of (column j, rows 8q .. 8q + 7)
+        // pass 2: the digits of (column j, rows 8q .. 8q + 7).  Eight
+        // consecutive lanes take eight consecutive columns at the same q:
+        // the raw column stride (528 = 16 mod 128) and the slices' swizzle
+        // then put their 16-byte loads and stores in eight different bank
+        // groups.
         for (int u = p; u < 1024; u += OZG_NPROD) {
-          const int j = u >> 3, q = u & 7;
-          const int4 pa = *(const int4*)&part[8 * j], pb = *(const int4*)&part[8 * j + 4];
-          const int E = max(max(max(pa.x, pa.y), max(pa.z, pa.w)), max(max(pb.x, pb.y), max(pb.z, pb.w)));
+          const int j = (u & 7) | ((u >> 6) << 3), q = (u >> 3) & 7;
+          const int E = cexp[c & 3][j];
           const int kind = s_kind[j];
           // the eight rows' digits with FP32 arithmetic (integer fixed point
           // first for FP64 values, or for FP32 groups whose scale leaves the
@@ -271,13 +292,13 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
 #pragma unroll
           for (int t = 0; t < OZG_S; t++)
             *(uint4*)(adig + t * OZG_SLICE + off) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
-          if (q == 0) cexp[c & 3][j] = kind ? E : 0;
         }
         fence_proxy_async();
         mbar_arrive(&a_full);
         mbar_arrive(&raw_empty[slot]);
       }
-      named_bar(1, OZG_NPROD);  // part[] is rewritten by the next chunk's pass 1
+      // no barrier here: the next chunk's pass 1 writes another scale slot
+      // and reads the other raw buffer
     }
   } else if (warp == 0 && lane == 0) {
     // ------------------------------------------------------- MMA issuer
