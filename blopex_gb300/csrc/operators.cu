@@ -847,10 +847,11 @@ static int st7_ring_ok(const gpu_Operator* op, const blk_cols* xc, int w)
   return 1;
 }
 
-// the tensor-map encoder of the driver, found once through the runtime
-static PFN_cuTensorMapEncodeTiled_v12000 st7t_encoder(void)
+// the tensor-map encoder of the driver (cuTensorMapEncodeTiled), found once
+// through the runtime; NULL when the driver has none
+extern "C" void* gb_tensormap_encoder(void)
 {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = NULL;
+  static void* fn = NULL;
   static int tried = 0;
   if (!tried) {
     tried = 1;
@@ -859,9 +860,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 st7t_encoder(void)
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+      fn = p;
   }
   return fn;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 st7t_encoder(void)
+{
+  return (PFN_cuTensorMapEncodeTiled_v12000)gb_tensormap_encoder();
 }
 
 // tensor maps of the FP32 block X as (x, y, z, column) for st7_tma_kernel:

@@ -21,8 +21,11 @@
 // Tile b of the grid pairs L with Q_b: the A operand has 128 rows, L's
 // columns in rows 0-63 and Q_b's in rows 64-127; the B operand is rows 0-63
 // of the same slices (L).  Per CTA (one per SM):
-//   warp 1          bulk-copies a chunk's columns (cp.async.bulk, 64 rows
-//                   each) into one of two raw buffers;
+//   warp 1          copies a chunk's columns into one of two raw buffers:
+//                   a run of equally spaced columns (a block's columns at
+//                   its leading dimension) as one 2-D TMA tile, other
+//                   columns one cp.async.bulk each (the per-request cost of
+//                   128 column copies per chunk otherwise bounds the kernel);
 //   warps 2-3, 12-15 find each column's chunk scale and write the digit
 //                   slices (128-byte-swizzled K-major, K = the chunk's rows);
 //   warp 0          allocates TMEM; one thread issues tcgen05.mma.kind::f16
@@ -32,6 +35,8 @@
 //                   column of [L Q_b]; warps w and w + 4 share TMEM lanes and
 //                   take 32 of the 64 L columns each).
 // Every wait is bounded; a timeout sets an error word, the outputs become NaN.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -45,20 +50,42 @@
 #define OZG_THREADS 512
 #define OZG_NPROD 192
 #define OZG_ROWS 64                      // rows per chunk
-#define OZG_COLSTRIDE 528                // raw bytes per column (64 FP64 + 16 padding)
-#define OZG_RAW (128 * OZG_COLSTRIDE)    // one raw buffer
+// a staged column: 64 rows and 16 bytes more, so that consecutive columns
+// start 16 bytes apart modulo 128 (different shared-memory bank groups); a
+// TMA tile of 66 FP64 / 68 FP32 rows lands its columns at exactly this stride
+#define OZG_STRIDE64 528
+#define OZG_STRIDE32 272
+#define OZG_RAW 69632                    // one raw buffer: 128 columns + run alignment
 #define OZG_SLICE 16384                  // 128 operand rows x 128 bytes
 #define OZG_SMEM (2 * OZG_RAW + OZG_S * OZG_SLICE + 1024)
 #define OZG_MAXQ 4  // 64 + 64 * OZG_MAXQ column slots fit blk_cols
+#define OZG_MAXMAPS 12
 
 struct ozg_params {
+  CUtensorMap maps[OZG_MAXMAPS];  // 2-D tiles (rows x columns) of equally spaced column runs
   blk_cols cols;       // tile b: L column c at cols.col[c]; Q_b column j at cols.col[64 + 64 b + j]
   int h, nq, ldt;                   // ldt: dtype of L (GPU_MV_*)
   int qw[OZG_MAXQ], qdt[OZG_MAXQ];  // widths and dtypes (GPU_MV_*) of the Q blocks
+  int nmaps;
+  int map_tile[OZG_MAXMAPS];   // the tile a map serves; -1: L, every tile
+  int map_slot[OZG_MAXMAPS];   // its first column slot
+  int map_bytes[OZG_MAXMAPS];  // bytes one load brings (the whole box)
+  unsigned short roff[OZG_MAXQ][128];   // raw-buffer offset of each slot, 16-byte units
+  unsigned char by_map[OZG_MAXQ][128];  // 1: the slot arrives with a map's tile
   long n;
   double* partial;  // [tile][cta][128][64]
   int* err;
 };
+
+// rows x columns tile of a column run: x = first row, the run's columns all
+static __device__ __forceinline__ void ozg_tile_load(uint32_t dst, const CUtensorMap* map, int x, uint64_t* bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(x), "r"(0), "r"(smem_u32(bar))
+      : "memory");
+}
 
 static __device__ __forceinline__ int ozg_col_kind(const ozg_params& prm, int b, int j, const void** ptr)
 {
@@ -95,7 +122,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = smem_align1024(smem_raw);
-  unsigned char* raws = smem;                  // [2][128 columns][528 B]
+  unsigned char* raws = smem;                  // [2][OZG_RAW]: columns at s_off
   unsigned char* adig = smem + 2 * OZG_RAW;    // [S][128 rows][128 B]
   __shared__ uint64_t raw_full[2], raw_empty[2], a_full, a_empty, acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base;
@@ -104,6 +131,8 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   // memory: a runtime index into the kernel-parameter table is slow
   __shared__ const void* s_col[128];
   __shared__ int s_kind[128];
+  __shared__ int s_off[128];   // raw-buffer offset of each column
+  __shared__ int s_copy[128];  // the column's own bulk copy: 0 none, 1 FP32, 2 FP64
   __shared__ int cexp[4][128];     // chunk scales, by chunk modulo 4
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -113,8 +142,11 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
 
   if (tid < 128) {
     const void* ptr = nullptr;
-    s_kind[tid] = ozg_col_kind(prm, b, tid, &ptr);
+    const int kind = ozg_col_kind(prm, b, tid, &ptr);
+    s_kind[tid] = kind;
     s_col[tid] = ptr;
+    s_off[tid] = 16 * (int)prm.roff[b][tid];
+    s_copy[tid] = prm.by_map[b][tid] ? 0 : kind;
   }
   if (tid == 0) {
     abort_flag = 0;
@@ -144,11 +176,14 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
   if (warp == 1) {
     // ------------------------------------------------------- bulk copies
     long issued[2] = {0, 0};  // chunks issued per slot
-    int ncol8 = 0, ncol4 = 0;  // FP64 and FP32 columns of this tile
+    int ncol8 = 0, ncol4 = 0;  // FP64 and FP32 columns copied one by one
     for (int j = 0; j < 128; j++) {
-      ncol8 += s_kind[j] == 2;
-      ncol4 += s_kind[j] == 1;
+      ncol8 += s_copy[j] == 2;
+      ncol4 += s_copy[j] == 1;
     }
+    uint32_t mapbytes = 0;  // the tiles of this CTA's runs
+    for (int m = 0; m < prm.nmaps; m++)
+      if (prm.map_tile[m] < 0 || prm.map_tile[m] == b) mapbytes += (uint32_t)prm.map_bytes[m];
     for (long c = 0; c < my_chunks; c++) {
       const int slot = (int)(c & 1);
       int stop = 0;
@@ -164,17 +199,21 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
       const long rows = min((long)OZG_ROWS, prm.n - r0);
       // every column's copy covers whole 16-byte pieces
       const uint32_t b8 = (uint32_t)(((rows + 1) & ~1L) * 8), b4 = (uint32_t)(((rows + 3) & ~3L) * 4);
-      const uint32_t total = (uint32_t)ncol8 * b8 + (uint32_t)ncol4 * b4;
+      // (a tile counts its whole box, rows past n included: they read as 0)
+      const uint32_t total = mapbytes + (uint32_t)ncol8 * b8 + (uint32_t)ncol4 * b4;
       if (lane == 0) mbar_expect_tx(&raw_full[slot], total);
       __syncwarp();
       unsigned char* raw = raws + slot * OZG_RAW;
+      for (int m = lane; m < prm.nmaps; m += 32)
+        if (prm.map_tile[m] < 0 || prm.map_tile[m] == b)
+          ozg_tile_load(smem_u32(raw + s_off[prm.map_slot[m]]), &prm.maps[m], (int)r0, &raw_full[slot]);
       for (int j = lane; j < 128; j += 32) {
         const void* ptr = s_col[j];
-        const int kind = s_kind[j];
+        const int kind = s_copy[j];
         if (kind == 2)
-          bulk_g2s(raw + j * OZG_COLSTRIDE, (const double*)ptr + r0, b8, &raw_full[slot]);
+          bulk_g2s(raw + s_off[j], (const double*)ptr + r0, b8, &raw_full[slot]);
         else if (kind == 1)
-          bulk_g2s(raw + j * OZG_COLSTRIDE, (const float*)ptr + r0, b4, &raw_full[slot]);
+          bulk_g2s(raw + s_off[j], (const float*)ptr + r0, b4, &raw_full[slot]);
       }
       issued[slot] = c + 1;
     }
@@ -207,7 +246,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
         const int nr = min(8, rows - 8 * q);
         int e = 0;
         if (kind == 2) {
-          const unsigned char* src = raw + j * OZG_COLSTRIDE + 64 * q;
+          const unsigned char* src = raw + s_off[j] + 64 * q;
 #pragma unroll
           for (int x = 0; x < 4; x++) {
             const int xx = (x + (q >> 1)) & 3;  // rows 2 xx, 2 xx + 1
@@ -216,7 +255,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
             if (2 * xx + 1 < nr) e = max(e, oz_bexp64(d.y));
           }
         } else if (kind == 1) {
-          const unsigned char* src = raw + j * OZG_COLSTRIDE + 32 * q;
+          const unsigned char* src = raw + s_off[j] + 32 * q;
 #pragma unroll
           for (int x = 0; x < 2; x++) {
             const int hx = x ^ ((q >> 2) & 1);  // rows 4 hx .. 4 hx + 3
@@ -246,7 +285,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
         tc_fence_after();
         // pass 2: the digits of (column j, rows 8q .. 8q + 7).  Eight
         // consecutive lanes take eight consecutive columns at the same q:
-        // the raw column stride (528 = 16 mod 128) and the slices' swizzle
+        // the raw column stride (528 or 272, 16 mod 128) and the slices' swizzle
         // then put their 16-byte loads and stores in eight different bank
         // groups.
         for (int u = p; u < 1024; u += OZG_NPROD) {
@@ -261,7 +300,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
           const int nr = min(8, rows - 8 * q);
           if (kind == 1) {
             float v[8];
-            ozg_load8(raw + j * OZG_COLSTRIDE + 32 * q, v);
+            ozg_load8(raw + s_off[j] + 32 * q, v);
 #pragma unroll
             for (int x = 0; x < 8; x++) v[x] = x < nr ? v[x] : 0.0f;
             if (sc != 0.0f) {
@@ -274,7 +313,7 @@ __global__ void __launch_bounds__(OZG_THREADS, 1) oz_gram_kernel(const __grid_co
             }
           } else if (kind == 2) {
             double v[8];
-            ozg_load8(raw + j * OZG_COLSTRIDE + 64 * q, v);
+            ozg_load8(raw + s_off[j] + 64 * q, v);
 #pragma unroll
             for (int x = 0; x < 8; x++) oz_digits4x8_f64(x < nr ? v[x] : 0.0, E, dg[x]);
           } else {
@@ -450,6 +489,87 @@ __global__ void oz_gram_reduce_kernel(const double* __restrict__ partial, int gx
   G[i + (size_t)col * ldg] = s;
 }
 
+// columns from slot s0 equally spaced by a stride that a tensor map can
+// take (a multiple of 16 bytes, at least a column's bytes): the run's length
+// (1 when the next column breaks it)
+static int ozg_run_length(const void* const* col, int s0, int maxlen, long colbytes)
+{
+  if (maxlen < 2) return 1;
+  const intptr_t d = (const char*)col[s0 + 1] - (const char*)col[s0];
+  if (d <= 0 || d % 16 || d < colbytes || d >= ((intptr_t)1 << 40)) return 1;
+  int r = 2;
+  while (r < maxlen && (const char*)col[s0 + r] - (const char*)col[s0 + r - 1] == d) r++;
+  return r;
+}
+
+// a tensor map of the run of r columns from prm->cols.col[s0] (column slot
+// `local` of the tile's staging buffer): tiles of 66 FP64 or 68 FP32 rows by
+// r columns (rows past n read as 0); 1 when encoded
+static int ozg_encode(PFN_cuTensorMapEncodeTiled_v12000 enc, ozg_params* prm, int tile, int s0, int local, int r,
+                      int f64)
+{
+  if (prm->nmaps >= OZG_MAXMAPS) return 0;
+  const int rows_box = f64 ? OZG_STRIDE64 / 8 : OZG_STRIDE32 / 4;
+  const cuuint64_t dims[2] = {(cuuint64_t)prm->n, (cuuint64_t)r};
+  const cuuint64_t strides[1] = {
+      (cuuint64_t)((const char*)prm->cols.col[s0 + 1] - (const char*)prm->cols.col[s0])};
+  const cuuint32_t box[2] = {(cuuint32_t)rows_box, (cuuint32_t)r}, es[2] = {1, 1};
+  if (enc(&prm->maps[prm->nmaps], f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+          (void*)prm->cols.col[s0], dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 0;
+  prm->map_tile[prm->nmaps] = tile;
+  prm->map_slot[prm->nmaps] = local;
+  prm->map_bytes[prm->nmaps] = rows_box * r * (f64 ? 8 : 4);
+  prm->nmaps++;
+  return 1;
+}
+
+// the staging layout of every tile: L's columns first at their stride, then
+// Q_b's; a run of at least two equally spaced columns becomes one tile load
+// (its start 128-byte aligned, as TMA wants), other columns are copied one
+// by one (all of them without the driver's encoder, or for short columns)
+static int ozg_layout(gpu_Context* ctx, ozg_params* prm, int ntiles)
+{
+  PFN_cuTensorMapEncodeTiled_v12000 enc = (PFN_cuTensorMapEncodeTiled_v12000)gb_tensormap_encoder();
+  if (prm->n < 128 || prm->n >= (1L << 31) - 128) enc = NULL;  // row coordinates are 32-bit
+  prm->nmaps = 0;
+  const int lf64 = prm->ldt == GPU_MV_FLOAT64, sl = lf64 ? OZG_STRIDE64 : OZG_STRIDE32;
+  int lmap = 0;
+  if (enc && prm->h >= 2 && ozg_run_length(prm->cols.col, 0, prm->h, prm->n * (lf64 ? 8 : 4)) == prm->h)
+    lmap = ozg_encode(enc, prm, -1, 0, 0, prm->h, lf64);
+  for (int t = 0; t < ntiles; t++) {
+    for (int c = 0; c < prm->h; c++) {
+      prm->roff[t][c] = (unsigned short)(c * sl / 16);
+      prm->by_map[t][c] = (unsigned char)lmap;
+    }
+    long off = ((long)prm->h * sl + 127) & ~127L;
+    const int w = t < prm->nq ? prm->qw[t] : 0;
+    const int qf64 = t < prm->nq && prm->qdt[t] == GPU_MV_FLOAT64, sq = qf64 ? OZG_STRIDE64 : OZG_STRIDE32;
+    for (int j = 0; j < w;) {
+      const int s0 = 64 + 64 * t + j;
+      const int r = enc ? ozg_run_length(prm->cols.col, s0, w - j, prm->n * (qf64 ? 8 : 4)) : 1;
+      const long at = (off + 127) & ~127L;
+      if (r >= 2 && at + (long)r * sq <= OZG_RAW && ozg_encode(enc, prm, t, s0, 64 + j, r, qf64)) {
+        for (int i = 0; i < r; i++) {
+          prm->roff[t][64 + j + i] = (unsigned short)((at + (long)i * sq) / 16);
+          prm->by_map[t][64 + j + i] = 1;
+        }
+        off = at + (long)r * sq;
+        j += r;
+        continue;
+      }
+      prm->roff[t][64 + j] = (unsigned short)(off / 16);
+      prm->by_map[t][64 + j] = 0;
+      off += sq;
+      j++;
+    }
+    if (off > OZG_RAW) return gb_fail(ctx, "oz_gram: tile %d needs %ld bytes of staging", t, off);
+  }
+  return 0;
+}
+
 extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, int ldt, int nq,
                           const blk_cols* Q, const int* qw, const int* qdt, double* G, int ldg)
 {
@@ -491,6 +611,7 @@ extern "C" int gb_oz_gram(gpu_Context* ctx, long n, const blk_cols* L, int h, in
   prm.nq = nq;
   qoff.q[nq] = wtot;
   const int ntiles = nq > 0 ? nq : 1;
+  if (ozg_layout(ctx, &prm, ntiles)) return -1;
   const long nchunks = (n + OZG_ROWS - 1) / OZG_ROWS;
   long gx = ctx->num_sms / ntiles;
   if (gx < 1) gx = 1;
