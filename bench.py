@@ -22,7 +22,10 @@ roofline = the kernel class with the largest share of the timed region,
          from the library's CUDA-event timers (algorithmic bytes per launch /
          event-timed duration), against MEASURED_PEAKS.json;
 cpu_baseline = the C restatement of the reference (oracle/, scalar loops,
-         one core) on a bounded sample, scaled to the full workload.
+         one core) on a bounded sample, scaled to the full workload;
+adjoint = the c4 derivative configuration (2D diffusion 512^2, forward solve
+         + reverse-mode gradient) measured once beside the headline: forward
+         and backward times and their ratio (--no-adjoint skips it).
 
 --impl reference times that CPU implementation alone (the reference's own
 algorithm on one host core, its LAPACK calls single-threaded; the compiled
@@ -79,7 +82,7 @@ CONFIGS = {
     # the same operator family at 128^3: a full solve takes seconds, so it can
     # be repeated as the timed step; the 256^3 case runs once beside it
     "c3m": dict(kind="stencil7", grid=(128, 128, 128), k=64, seed=2, tol=1e-8, maxit=1000,
-                jacobi=True, precond="pcg20", full="c3", fp64_iterations=176,
+                jacobi=True, precond="pcg20", full="c3", fp64_iterations=176, adjoint="c4",
                 label="matrix-free variable-coefficient 7-point stencil 128^3 (n=2097152), face "
                       "coefficients exp(N(0,1)) seed 2, k=64, X0 drand48 seed 2, tol 1e-8, "
                       "preconditioner 20 Jacobi-CG steps on A"),
@@ -312,11 +315,22 @@ def run_adjoint(args, cfg):
     stream); e2e = the torch.autograd path from a host theta to host
     d loss / d theta."""
     import torch
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    line = measure_adjoint(cfg, args.steps, args.warmup, world, local, dist)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def measure_adjoint(cfg, steps, warmup, world, local, dist):
+    """The adjoint configuration's measurement (its JSON line as a dict):
+    `warmup` untimed forward + backward steps, then `steps` timed ones."""
+    import torch
     from blopex_gb300 import adjoint as AD
     from blopex_gb300 import problems as P
     from blopex_gb300 import solver as S
-    world, rank, local, dist = dist_setup()
-    torch.cuda.set_device(local)
     nx, ny = cfg["grid"]
     n, k = nx * ny, cfg["k"]
     theta = 0.5 * P.gaussian_random_field(nx, ny, 0.1, cfg["seed"])
@@ -355,7 +369,7 @@ def run_adjoint(args, cfg):
         torch.cuda.synchronize()
         return out, e0.elapsed_time(e1)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         backward(forward())
     ctx.profiling(True)
     ctx.reset_kernel_times()
@@ -365,7 +379,7 @@ def run_adjoint(args, cfg):
     sampler.start()
     launches0 = ctx.lib.gpu_KernelLaunchCount()
     fwd, bwd, its, aits, res = [], [], 0, 0, 0.0
-    for _ in range(args.steps):
+    for _ in range(steps):
         r, tf = timed(forward)
         (adj, g), tb = timed(backward, r)
         fwd.append(tf)
@@ -383,7 +397,7 @@ def run_adjoint(args, cfg):
                            adjoint_maxit=20000, inner_cg=cfg["inner_cg"])
     vt = torch.from_numpy(v)
     e2e = []
-    for _ in range(max(1, args.steps)):
+    for _ in range(max(1, steps)):
         th = torch.from_numpy(theta).requires_grad_(True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -397,7 +411,7 @@ def run_adjoint(args, cfg):
     total = top_level_ms(kt)
     e2e_ms = max_over_ranks(statistics.median(e2e), dist, "cuda")
     line = {"metric": "fwd+bwd ms (forward solve + reverse-mode gradient)", "value": tf + tb,
-            "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "unit": "ms", "n_gpus": world, "steps": steps, "warmup": warmup,
             "ms_per_step": tf + tb, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["label"], "n": n, "k": k, "tol": cfg["tol"],
@@ -414,10 +428,7 @@ def run_adjoint(args, cfg):
                     "d2h_bytes_per_step": 8 * (n * k + k + cx.size + cy.size)},
             "gpu_launches": int(launches), "clocks": clocks,
             "roofline": None}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    return line
 
 
 def run_generalized(args, cfg):
@@ -659,6 +670,8 @@ def main():
     ap.add_argument("--no-other-arm", action="store_true",
                     help="skip the other precision's arm (FP64 beside mixed or the reverse)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the derivative configuration measured beside the headline")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
     if args.maxit:
@@ -868,10 +881,30 @@ def main():
         if full and full.get("fp64"):
             line["full_size"]["cpu_baseline"] = cpu_baseline(dict(CONFIGS[cfg["full"]]),
                                                              full["fp64"]["iterations"])
+    if cfg.get("adjoint") and not args.no_adjoint:
+        line["adjoint"] = adjoint_summary(cfg["adjoint"], world, local, dist)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def adjoint_summary(name, world, local, dist):
+    """The derivative configuration measured once beside the headline (one
+    untimed and one timed forward + backward step): its forward and backward
+    times, their ratio and the end-to-end autograd time.  A failure here is
+    reported in the record and does not touch the headline."""
+    try:
+        a = measure_adjoint(dict(CONFIGS[name]), 1, 1, world, local, dist)
+    except Exception as e:  # the headline line is printed whatever happens here
+        return {"config": name, "error": f"{type(e).__name__}: {e}"}
+    return {"config": name, "workload": a["config"]["workload"], "forward_ms": a["forward_ms"],
+            "backward_ms": a["backward_ms"], "fwd_plus_bwd_ms": a["value"],
+            "fwd_plus_bwd_over_fwd": a["fwd_plus_bwd_over_fwd"],
+            "lobpcg_iterations": a["lobpcg_iterations"],
+            "adjoint_cg_iterations": a["adjoint_cg_iterations"],
+            "adjoint_max_rel_residual": a["adjoint_max_rel_residual"], "e2e_ms": a["e2e"]["value"],
+            "gpu_launches": a["gpu_launches"], "steps": 1, "warmup": 1}
 
 
 def run_full(cfg, ctx, S, torch, stream, precond):
