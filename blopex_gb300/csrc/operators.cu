@@ -848,20 +848,19 @@ static int st7_ring_ok(const gpu_Operator* op, const blk_cols* xc, int w)
 }
 
 // the tensor-map encoder of the driver (cuTensorMapEncodeTiled), found once
-// through the runtime; NULL when the driver has none
+// through the runtime (a function-local static: initialised once, also when
+// several host threads ask first); NULL when the driver has none
 extern "C" void* gb_tensormap_encoder(void)
 {
-  static void* fn = NULL;
-  static int tried = 0;
-  if (!tried) {
-    tried = 1;
+  static void* const fn = [] {
     void* p = NULL;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = p;
-  }
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = NULL;
+    return p;
+  }();
   return fn;
 }
 
