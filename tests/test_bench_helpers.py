@@ -65,3 +65,23 @@ def test_nested_rayleigh_ritz_stages_stay_out_of_the_total():
 def test_reference_arm_scales_by_the_recorded_fp64_iteration_count():
     assert bench.CONFIGS["c3m"]["fp64_iterations"] == 176
     assert bench.CONFIGS["c3"]["fp64_iterations"] == 565
+
+
+def test_adjoint_record_keeps_its_fields_and_reports_failures(monkeypatch):
+    """The derivative record beside the headline carries the forward and
+    backward times of the adjoint configuration's line; a failure there
+    becomes an error field instead of ending the run."""
+    fake = {"config": {"workload": "w"}, "forward_ms": 100.0, "backward_ms": 25.0, "value": 125.0,
+            "fwd_plus_bwd_over_fwd": 1.25, "lobpcg_iterations": 9, "adjoint_cg_iterations": 4,
+            "adjoint_max_rel_residual": 1e-9, "e2e": {"value": 130.0}, "gpu_launches": 7}
+    monkeypatch.setattr(bench, "measure_adjoint", lambda *a, **k: fake)
+    rec = bench.adjoint_summary("c4", 1, 0, None)
+    assert rec["config"] == "c4" and rec["fwd_plus_bwd_ms"] == 125.0
+    assert rec["fwd_plus_bwd_over_fwd"] == 1.25 and rec["e2e_ms"] == 130.0
+
+    def boom(*a, **k):
+        raise RuntimeError("no device")
+    monkeypatch.setattr(bench, "measure_adjoint", boom)
+    rec = bench.adjoint_summary("c4", 1, 0, None)
+    assert rec == {"config": "c4", "error": "RuntimeError: no device"}
+    assert bench.CONFIGS["c3m"]["adjoint"] == "c4" and bench.CONFIGS["c4"]["kind"] == "adjoint5"
