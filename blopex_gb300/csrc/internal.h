@@ -89,7 +89,7 @@ void gb_pool_put(gpu_Context* ctx, void* p, size_t bytes);
 int gb_fail(gpu_Context* ctx, const char* fmt, ...);
 int gb_cuda_check(gpu_Context* ctx, int cuda_status, const char* what);
 void* gb_workspace(gpu_Context* ctx, size_t bytes);
-/* the driver's cuTensorMapEncodeTiled (operators.cu), NULL when absent */
+/* the CUDA driver's cuTensorMapEncodeTiled (operators.cu), NULL when absent */
 void* gb_tensormap_encoder(void);
 void* gb_pinned(gpu_Context* ctx, size_t bytes);
 void gb_count_launch(long long n);

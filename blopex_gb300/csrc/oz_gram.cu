@@ -529,7 +529,7 @@ static int ozg_encode(PFN_cuTensorMapEncodeTiled_v12000 enc, ozg_params* prm, in
 // the staging layout of every tile: L's columns first at their stride, then
 // Q_b's; a run of at least two equally spaced columns becomes one tile load
 // (its start 128-byte aligned, as TMA wants), other columns are copied one
-// by one (all of them without the driver's encoder, or for short columns)
+// by one (all of them without the CUDA driver's encoder, or for short columns)
 static int ozg_layout(gpu_Context* ctx, ozg_params* prm, int ntiles)
 {
   PFN_cuTensorMapEncodeTiled_v12000 enc = (PFN_cuTensorMapEncodeTiled_v12000)gb_tensormap_encoder();

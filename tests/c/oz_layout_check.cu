@@ -1,7 +1,7 @@
 // Host-only check of the split Gram's staging layout (ozg_layout in
 // blopex_gb300/csrc/oz_gram.cu): no GPU is used.  The kernel source is
 // included for its host code; the library functions it calls are stubbed
-// and the driver's tensor-map encoder is replaced by one that checks its
+// and the CUDA driver's tensor-map encoder is replaced by one that checks its
 // arguments the way the driver documents them (16-byte aligned base and
 // strides, box dimensions of at most 256) and succeeds.
 //
