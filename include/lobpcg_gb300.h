@@ -241,7 +241,14 @@ int gpu_BlockUpdate(gpu_MultiVector* X, const double* C_host, int ldc, gpu_Multi
    (nq <= 4).  G_host (h x (h + sum of the Q widths), leading dimension ldg)
    receives L'L and then each L'Q_b.  The Gram blocks of the reference's
    gramA / gramB (serial_Multi_VectorInnerProd, multi_vector.c:354-406, at
-   lobpcg.c:1092-1160) as the mixed mode forms them. */
+   lobpcg.c:1092-1160) as the mixed mode forms them.  Range: the chunk sums
+   are scaled and accumulated in FP32 pairs, so the accuracy holds while, in
+   every 64-row chunk, the product of two columns' largest magnitudes lies
+   between 2^-120 and 2^100 (for instance every entry within [2^-60, 2^50]
+   in magnitude; the solver's blocks -- unit columns and their images -- are
+   well inside).  Outside it entries lose accuracy or overflow; a column
+   whose chunk maximum is below 2^-118 or at least 2^135 counts as zero in
+   that chunk. */
 int gpu_SplitGram(gpu_MultiVector* L, gpu_MultiVector** Q, int nq, double* G_host, int ldg);
 
 /* ---------------------------------------------------------------- */
