@@ -114,3 +114,39 @@ def test_inaccurate_outside_it():
                                                                           y0 * 2.0 ** -70)
     large = split_gram_entry(x0 * 2.0 ** 70, y0 * 2.0 ** 70)      # products near 2^144
     assert not np.isfinite(large)
+
+
+# ------------------------------------------------ the update (oz_xc.cu)
+def split_update_entry(xrow, ccol):
+    """Y_ij of oz_xc restated: the row's and the column's scales, six 7-bit
+    digits of each value (three exact 14-bit parts of the 42-bit fixed point
+    for X, balanced digits for C), the levels t + u <= 5 summed exactly, the
+    integer rounded once to FP64 and scaled by 2^(er + ec - 2093)."""
+    from tests.test_split_digits import bexp64, fixed64, update_c_digits, update_x_digits
+    er, ec = max(map(bexp64, xrow)), max(map(bexp64, ccol))
+    if er == 0 or ec == 0:
+        return 0.0
+    T = 0
+    for xv, cv in zip(xrow, ccol):
+        _, dx = update_x_digits(xv, er)
+        dc = update_c_digits(fixed64(cv, ec, F=42), cv < 0)
+        for t in range(6):
+            for u in range(6 - t):
+                T += int(dx[t]) * int(dc[u]) * 128 ** (5 - t - u)
+    return float(T) * 2.0 ** (er + ec - 2093)
+
+
+def test_update_restated_meets_its_bound_over_the_fp64_range():
+    """|Y - X C| <= h 2^-38 rowmax|X| colmax|C| (plus the final rounding):
+    the update recombines in integers and scales on the FP64 exponent field,
+    so the bound holds across the FP64 range, unlike the Gram's FP32 pairs."""
+    rng = np.random.default_rng(5)
+    h = 64
+    for sx, sc in ((0, 0), (-300, 250), (400, -380), (-60, -60), (90, 90)):
+        for _ in range(3):
+            x = rng.standard_normal(h) * np.exp(3 * rng.standard_normal(h)) * 2.0 ** sx
+            c = rng.standard_normal(h) * np.exp(3 * rng.standard_normal(h)) * 2.0 ** sc
+            y = split_update_entry(x, c)
+            ex = _exact(x, c)
+            bound = h * 2.0 ** -38 * np.abs(x).max() * np.abs(c).max()
+            assert abs(y - ex) <= bound + abs(ex) * 2.0 ** -52, (sx, sc, y, ex)
