@@ -77,6 +77,13 @@ struct ozg_params {
   int* err;
 };
 
+// a kernel parameter block of at most 32,764 bytes; raw buffers that keep the
+// digit slices behind them 1024-byte aligned (the MMA descriptors' swizzle
+// atom); dynamic plus static shared memory within the 227 KB of a CTA
+static_assert(sizeof(ozg_params) <= 32764, "oz_gram parameters exceed the kernel parameter space");
+static_assert(OZG_RAW % 1024 == 0, "raw buffers must keep the digit slices 1024-byte aligned");
+static_assert(OZG_SMEM + 8192 <= 232448, "oz_gram shared memory exceeds a CTA's 227 KB");
+
 // rows x columns tile of a column run: x = first row, the run's columns all
 static __device__ __forceinline__ void ozg_tile_load(uint32_t dst, const CUtensorMap* map, int x, uint64_t* bar)
 {
