@@ -3,7 +3,8 @@
 // included for its host code; the library functions it calls are stubbed
 // and the CUDA driver's tensor-map encoder is replaced by one that checks its
 // arguments the way the driver documents them (16-byte aligned base and
-// strides, box dimensions of at most 256) and succeeds.
+// strides, box dimensions of at most 256) and succeeds, except on every fifth
+// call (the fallback to per-column copies).
 //
 // For random L and Q blocks -- contiguous with a padded leading dimension,
 // masked (columns skipped), scattered, merged from several blocks, FP32 and
@@ -33,6 +34,9 @@ static CUresult check_encoder(CUtensorMap* m, CUtensorMapDataType, cuuint32_t ra
   if (rank != 2 || ((uintptr_t)base & 15) || strides[0] % 16 || box[0] == 0 || box[0] > 256 || box[1] == 0 ||
       box[1] > 256 || box[1] != dims[1] || es[0] != 1 || es[1] != 1)
     return CUDA_ERROR_INVALID_VALUE;
+  // every fifth call fails as well: the layout must then copy those columns
+  // one by one (and may try a shorter run from the next column)
+  if (g_encoder_calls % 5 == 0) return CUDA_ERROR_INVALID_VALUE;
   memset(m, 0, sizeof *m);
   return CUDA_SUCCESS;
 }
